@@ -1,0 +1,197 @@
+"""ctypes wrapper of the CPU oracle (gbo_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / reference legs of bench.py, always as the checker or the timed
+CPU baseline.  The product package never imports this module.
+
+Boxes are numpy int32 arrays of shape (n, 4) holding x1, y1, x2, y2.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "libgbo_oracle.so")
+_REF = os.path.join(_HERE, "_ref", "libref_sort.so")
+
+XOR, OR, AND, NOT, MERGE = 0, 1, 2, 3, 4
+
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle (and the reference CPU sort helpers when mounted)."""
+    if force or not os.path.exists(_LIB):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "_build/libgbo_oracle.so"])
+    subprocess.call(["make", "-s", "-C", _HERE, "ref"], stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            build()
+        L = ctypes.CDLL(_LIB)
+        P = ctypes.c_void_p
+        i64, i32 = ctypes.c_int64, ctypes.c_int32
+        L.orc_boolean.argtypes = [P, i64, P, i64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]
+        L.orc_boolean.restype = i64
+        L.orc_grow.argtypes = [P, i64, i32, i32, i32, i32, ctypes.c_int, ctypes.POINTER(P)]
+        L.orc_grow.restype = i64
+        L.orc_size.argtypes = [P, i64, i32, ctypes.c_int, ctypes.POINTER(P)]
+        L.orc_size.restype = i64
+        L.orc_union_area.argtypes = [P, i64]
+        L.orc_union_area.restype = i64
+        L.orc_components.argtypes = [P, i64, P]
+        L.orc_components.restype = i64
+        L.orc_morton_key.argtypes = [P]
+        L.orc_morton_key.restype = ctypes.c_uint64
+        L.orc_tracker_key.argtypes = [i32, i32]
+        L.orc_tracker_key.restype = ctypes.c_uint64
+        L.orc_um_to_dbu.argtypes = [ctypes.c_double]
+        L.orc_um_to_dbu.restype = i32
+        L.orc_op1.argtypes = [P, i64, i32, ctypes.c_int, P, P]
+        L.orc_op1.restype = None
+        L.orc_free.argtypes = [P]
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _arr(b):
+    b = np.ascontiguousarray(b, dtype=np.int32).reshape(-1, 4)
+    return b
+
+
+def _take(n, p):
+    if n < 0:
+        raise ValueError("oracle rejected an invalid box")
+    if n == 0:
+        lib().orc_free(p)
+        return np.zeros((0, 4), np.int32)
+    out = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_int32)), shape=(n * 4,))
+    res = out.copy().reshape(n, 4)
+    lib().orc_free(p)
+    return res
+
+
+def boolean(A, B, op, grid_log2=16):
+    A, B = _arr(A), _arr(B)
+    p = ctypes.c_void_p()
+    n = lib().orc_boolean(A.ctypes.data, len(A), B.ctypes.data, len(B), op, grid_log2, ctypes.byref(p))
+    return _take(n, p)
+
+
+def merge(A, grid_log2=16):
+    return boolean(A, np.zeros((0, 4), np.int32), MERGE, grid_log2)
+
+
+def grow(A, E, N, W, S, grid_log2=16):
+    A = _arr(A)
+    p = ctypes.c_void_p()
+    n = lib().orc_grow(A.ctypes.data, len(A), E, N, W, S, grid_log2, ctypes.byref(p))
+    return _take(n, p)
+
+
+def size(A, s, grid_log2=16):
+    A = _arr(A)
+    p = ctypes.c_void_p()
+    n = lib().orc_size(A.ctypes.data, len(A), s, grid_log2, ctypes.byref(p))
+    return _take(n, p)
+
+
+def union_area(A):
+    A = _arr(A)
+    return int(lib().orc_union_area(A.ctypes.data, len(A)))
+
+
+def components(A):
+    A = _arr(A)
+    labels = np.zeros(len(A), np.int64)
+    n = lib().orc_components(A.ctypes.data, len(A), labels.ctypes.data)
+    return int(n), labels
+
+
+def morton_keys(A):
+    A = _arr(A)
+    L = lib()
+    return np.array([L.orc_morton_key(A[i:i + 1].ctypes.data) for i in range(len(A))], np.uint64)
+
+
+def morton_keys_np(A):
+    """Vectorised restatement of the same key (numpy), for large arrays."""
+    A = _arr(A).astype(np.int64)
+    cx = ((A[:, 0] + A[:, 2]) // 2)
+    cy = ((A[:, 1] + A[:, 3]) // 2)
+    # C division truncates toward zero; numpy // floors: fix negative odd sums.
+    sx = A[:, 0] + A[:, 2]
+    sy = A[:, 1] + A[:, 3]
+    cx = np.where((sx < 0) & (sx % 2 != 0), cx + 1, cx)
+    cy = np.where((sy < 0) & (sy % 2 != 0), cy + 1, cy)
+    ux = (cx.astype(np.uint64) & np.uint64(0xFFFFFFFF)) ^ np.uint64(0x80000000)
+    uy = (cy.astype(np.uint64) & np.uint64(0xFFFFFFFF)) ^ np.uint64(0x80000000)
+
+    def spread(m):
+        m = (m | (m << np.uint64(16))) & np.uint64(0x0000FFFF0000FFFF)
+        m = (m | (m << np.uint64(8))) & np.uint64(0x00FF00FF00FF00FF)
+        m = (m | (m << np.uint64(4))) & np.uint64(0x0F0F0F0F0F0F0F0F)
+        m = (m | (m << np.uint64(2))) & np.uint64(0x3333333333333333)
+        m = (m | (m << np.uint64(1))) & np.uint64(0x5555555555555555)
+        return m
+
+    return (spread(uy) << np.uint64(1)) | spread(ux)
+
+
+def tracker_keys_np(X, Y):
+    ux = (np.asarray(X, np.int64).astype(np.uint64) & np.uint64(0xFFFFFFFF)) ^ np.uint64(0x80000000)
+    uy = (np.asarray(Y, np.int64).astype(np.uint64) & np.uint64(0xFFFFFFFF)) ^ np.uint64(0x80000000)
+    return (ux << np.uint64(32)) | uy
+
+
+def um_to_dbu(r):
+    return int(lib().orc_um_to_dbu(float(r)))
+
+
+def op1(A, amount=1, grid_log2=16):
+    """OP1 deck; returns (counts dict, union area)."""
+    A = _arr(A)
+    counts = np.zeros(8, np.int64)
+    area = np.zeros(1, np.int64)
+    lib().orc_op1(A.ctypes.data, len(A), amount, grid_log2, counts.ctypes.data, area.ctypes.data)
+    keys = ["poly_1", "poly_2", "outer_ring", "inner_ring", "ring_and1", "ring_intersection", "merged"]
+    return {k: int(counts[i]) for i, k in enumerate(keys)}, int(area[0])
+
+
+def canonical(A):
+    """Sort boxes by (x1, y1, x2, y2)."""
+    A = _arr(A)
+    if len(A) == 0:
+        return A
+    idx = np.lexsort((A[:, 3], A[:, 2], A[:, 1], A[:, 0]))
+    return A[idx]
+
+
+def area_of(A):
+    A = _arr(A).astype(np.int64)
+    return int(((A[:, 2] - A[:, 0]) * (A[:, 3] - A[:, 1])).sum())
+
+
+def xor_empty(A, B, grid_log2=16):
+    """Our XOR checker (stands in for boost_xor_checker.cpp:68-152): True iff
+    the point sets of A and B are equal."""
+    return len(boolean(A, B, XOR, grid_log2)) == 0
+
+
+def ref_sort_lib():
+    """The reference's own CPU sort helpers (gpu_morton.cu / event_sorter.cu,
+    #ifndef USE_GPU branch), compiled from the mounted sources into _ref/ by
+    the Makefile.  None when they were not built."""
+    if not os.path.exists(_REF):
+        return None
+    L = ctypes.CDLL(_REF)
+    L.thrust_sort_boxes_direct.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    L.thrust_sort_boxes_indirect.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    L.cpp_std_sort_trackers.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    return L
