@@ -65,13 +65,31 @@ def test_edge_cases(ctx, oracle):
                  (np.repeat(one, 7, axis=0), one),  # exact duplicates (SED_L122_D16 has some)
                  (np.array([[0, 0, 5, 5], [5, 0, 10, 5], [0, 5, 5, 10]], np.int32), one),  # edge touches
                  (np.array([[65535, 65535, 65537, 65537]], np.int32), one),  # straddles a tile corner
-                 (np.array([[-2147480000, -2147480000, -2147470000, -2147470000]], np.int32), big)]:
+                 (np.array([[-2000000000, -2000000000, -1999990000, -1999990000]], np.int32),
+                  np.array([[-1999000000, -1999995000, -1998000000, -1999993000]], np.int32)),
+                 (np.array([[-2000000, -2000000, -1990000, -1990000]], np.int32), big)]:
         for op in OPS + [4]:
             check(ctx, oracle, A, B, op)
     # A XOR A is empty, A NOT A is empty
     A = random_layer(5000, die=150000, seed=9)
     assert len(gpu_bool(ctx, A, A, 0)) == 0
     assert len(gpu_bool(ctx, A, A, 3)) == 0
+
+
+def test_tile_window_limit_is_an_error(ctx):
+    """A cell whose tile window exceeds 2^28 tiles (boxes ~4e9 dbu apart at
+    the default 65536-dbu grid) is refused with GB_ERR_CAPACITY, not run."""
+    from vlsi_layout_gb300 import engine
+    A = np.array([[-2147480000, -2147480000, -2147470000, -2147470000],
+                  [2147400000, 2147400000, 2147410000, 2147410000]], np.int32)
+    m = ctx.mark()
+    try:
+        with pytest.raises(engine.GBError) as ei:
+            ctx.op(4, ctx.layer(A)).to_numpy()
+        assert ei.value.code == engine.GB_ERR_CAPACITY
+    finally:
+        ctx.release(m)
+    ctx.sync()  # the error was reported once and cleared
 
 
 def test_golden_fixtures(ctx, oracle):

@@ -149,14 +149,13 @@ class Context:
 
     def _chk(self, rc):
         if rc != GB_OK:
-            raise GBError(rc, (lib().gb_last_error(self.h) or b"").decode())
+            msg = (lib().gb_last_error(self.h) or b"").decode()
+            lib().gb_clear_status(self.h)  # the error is reported once, by this exception
+            raise GBError(rc, msg)
 
     def sync(self):
         need = ctypes.c_int64()
-        rc = lib().gb_sync(self.h, ctypes.byref(need))
-        if rc != GB_OK:
-            lib().gb_clear_status(self.h)
-        self._chk(rc)
+        self._chk(lib().gb_sync(self.h, ctypes.byref(need)))
 
     def set_stream(self, stream_handle):
         self._chk(lib().gb_set_stream(self.h, ctypes.c_void_p(stream_handle)))
