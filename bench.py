@@ -1,0 +1,364 @@
+"""Benchmark: input boxes/s of the OP1 ring-check deck on a batched layout.
+
+Workload (one step): the OP1 deck (GROW 1 dbu, SIZE -1 dbu, two FRAME-NOTs,
+two ANDs, two ASSERT_ZEROs; op_template.m4:14-22) plus the Klee union area on
+every cell of a 4096-cell batched layout whose cells have lognormal box
+counts (median 8000, sigma 0.92, clipped to [100, 200000], ~50M boxes in
+total), each cell a seeded cfg0-style random layer (width/height uniform in
+[20, 2000] dbu, lower-left uniform in a die of side 1e6*sqrt(n/1e5)).
+
+  value     : batched form, inputs resident in HBM; the whole chain for all
+              cells is one CUDA-graph replay of persistent kernels.
+  e2e       : the same deck through the host C-ABI (gb_op1_host) from pinned
+              host buffers: H2D of the boxes, the chain, D2H of the per-cell
+              ASSERT_ZERO counts and areas, all inside the timed region.
+  plain     : the one-op-per-call drop-in (PerformBoostPolygonOperation /
+              PerformBoostPolygonMerge per cell and operator, host buffers),
+              timed on a sample of cells.
+  cpu_baseline / --impl reference : the CPU oracle (a C++/OpenMP restatement
+              of the reference's CPU path) on a bounded sample of cells.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+METRIC = "input boxes/s for OP1 deck on 1 GB300, batched vs plain GPU, bit-exact; p99 ms"
+
+
+def make_cells(ncell=4096, median=8000, sigma=0.92, lo=100, hi=200_000, seed=2):
+    """Batched-deck layout: per-cell lognormal box counts; each cell is a
+    cfg0-style random layer in a die scaled to its box count."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(rng.lognormal(np.log(median), sigma, ncell)), lo, hi).astype(np.int64)
+    total = int(counts.sum())
+    die = (1_000_000 * np.sqrt(counts / 100_000.0)).astype(np.int64)
+    die = np.maximum(die, 4000)
+    dbox = np.repeat(die, counts)
+    w = rng.integers(20, 2001, total)
+    h = rng.integers(20, 2001, total)
+    x = (rng.random(total) * (dbox - w)).astype(np.int64)
+    y = (rng.random(total) * (dbox - h)).astype(np.int64)
+    boxes = np.stack([x, y, x + w, y + h], axis=1).astype(np.int32)
+    off = np.zeros(ncell + 1, np.int64)
+    off[1:] = np.cumsum(counts)
+    return boxes, off
+
+
+def sample_cells(off, target_boxes):
+    """First k cells holding about target_boxes boxes."""
+    k = int(np.searchsorted(off, target_boxes))
+    return max(1, min(k, len(off) - 1))
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    def __init__(self, device=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per scanline-kernel launch from the committed ncu summary
+    (profiles/k_tile_op1_cells.md, line 'traffic_bytes_per_launch: N'), or None."""
+    p = os.path.join(ROOT, "profiles", "k_tile_op1_cells.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_leg(boxes, off, seconds=15.0):
+    """Time the CPU oracle's OP1 on the first cells (about `seconds` of work)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = int(O.lib().orc_num_threads())
+    k = sample_cells(off, 200_000)
+    t0 = time.perf_counter()
+    O.op1_cells(boxes[:off[k]], off[:k + 1] - off[0])
+    dt = time.perf_counter() - t0
+    rate = off[k] / dt
+    # grow the sample to about `seconds` of CPU work
+    k2 = sample_cells(off, int(rate * seconds))
+    if k2 > k:
+        t0 = time.perf_counter()
+        O.op1_cells(boxes[:off[k2]], off[:k2 + 1])
+        dt = time.perf_counter() - t0
+        k = k2
+    return {"value": float(off[k] / dt), "unit": "boxes/s", "cores": threads, "kind": "port",
+            "sample": "OP1 + union area on the first %d cells (%d boxes), %.1f s" % (k, int(off[k]), dt)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def run_reference(args, boxes, off, world, rank, dist):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    threads = int(O.lib().orc_num_threads())
+    k = sample_cells(off, args.ref_boxes)
+    sub, soff = boxes[:off[k]], off[:k + 1]
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        O.op1_cells(sub[:soff[min(4, k)]], soff[:min(4, k) + 1])
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        counts, area = O.op1_cells(sub, soff)
+        times.append(time.perf_counter() - t0)
+    dt = sum(times) / len(times)
+    v = float(soff[k] / dt)
+    fails = int((counts[:, 4] > 0).sum() + (counts[:, 5] > 0).sum())
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "boxes/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "OP1 deck + union area, batched cells (lognormal median 8000, 4096 cells); "
+                               "reference arm runs a bounded sample of cells per step",
+                   "cells": int(len(off) - 1), "boxes": int(off[-1]), "sample_cells": k,
+                   "sample_boxes": int(soff[k])},
+        "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": threads, "kind": "port",
+                         "sample": "OP1 + union area on the first %d cells (%d boxes) per step" % (k, int(soff[k]))},
+        "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "assert_zero_failures": fails,
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
+    ap.add_argument("--cells", type=int, default=4096)
+    ap.add_argument("--median", type=int, default=8000)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--plain-boxes", type=int, default=400_000)
+    ap.add_argument("--ref-boxes", type=int, default=600_000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_init()
+    boxes, off = make_cells(args.cells, args.median, seed=args.seed)
+    nbox = int(off[-1])
+    if args.impl == "reference":
+        run_reference(args, boxes, off, world, rank, dist)
+        return
+
+    import torch
+    from vlsi_layout_gb300 import engine
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    ctx = engine.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    P = ctx.layer(boxes, off)
+    ctx.sync()
+
+    # ---- capture the batched chain once (OP1 + union area), profiling events inside
+    mark = ctx.mark()
+    factor, scratch = 2, 8 << 20
+    for attempt in range(5):
+        ctx.profile(True)
+        ctx.graph_begin()
+        outs = ctx.op1(P, 1)
+        area_layer = ctx.op(engine.MERGE, P)  # strips of P; its cell_area is the union area
+        graph = ctx.graph_end()
+        for _ in range(args.warmup):
+            ctx.graph_launch(graph)
+        try:
+            ctx.sync()
+            break
+        except engine.GBError as e:
+            if e.code != engine.GB_ERR_CAPACITY or attempt == 4:
+                raise
+            engine.lib().gb_graph_destroy(graph)
+            ctx.release(mark)
+            mark = ctx.mark()
+            factor, scratch = factor * 2, scratch * 2
+            engine.lib().gb_set_capacity_factor(ctx.h, factor)
+            engine.lib().gb_set_tile_scratch(ctx.h, scratch)
+    nkern = int(engine.lib().gb_graph_kernels(graph))
+    counts = np.stack([L.count()[1] for L in outs], axis=1)
+    fails = int((counts[:, 4] > 0).sum() + (counts[:, 5] > 0).sum())
+
+    # ---- timed region
+    clk = Clocks(local)
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    engine.lib().gb_profile(ctx.h, 2)  # zero the byte counters, keep the graph's event pairs
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.graph_launch(graph)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t[0])
+    clocks = clk.stop()
+    ctx.sync()
+    tile_ms_last, tile_launches, bin_, bout = ctx.profile_read()
+    # events hold the last replay; byte counters accumulated over all timed replays
+    bytes_per_step = (bin_ + bout) / args.steps
+    ntile_per_step = max(1, tile_launches)
+    peak, peak_kind = peaks()
+    achieved = (bytes_per_step / (tile_ms_last / 1e3)) / 1e9 if tile_ms_last > 0 else None
+    traffic = ncu_traffic()
+
+    # ---- parity on sampled cells: per-cell layer counts and areas against the oracle
+    parity = "not checked"
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        ks = sample_cells(off, 60_000)
+        ec, ea = O.op1_cells(boxes[:off[ks]], off[:ks + 1])
+        ga = np.array(area_layer.count()[1])  # strips of P per cell (merge)
+        area_dev = ctx.area(P)[:ks]
+        ok = np.array_equal(counts[:ks], ec) and np.array_equal(area_dev, ea)
+        parity = "bit-exact counts (6 layers) and union area on %d sampled cells: %s" % (ks, "pass" if ok else "FAIL")
+        del ga
+    engine.lib().gb_graph_destroy(graph)
+    ctx.release(mark)
+
+    # ---- e2e through the host C-ABI (pinned buffers)
+    pinned = torch.from_numpy(boxes).pin_memory()
+    ctx.op1_host(pinned.data_ptr(), nbox, off, 1)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        c2, a2, f2 = ctx.op1_host(pinned.data_ptr(), nbox, off, 1)
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_ok = np.array_equal(c2, counts)
+
+    # ---- plain: one drop-in call per cell and operator, host buffers
+    kp = sample_cells(off, args.plain_boxes)
+    t0 = time.perf_counter()
+    for k in range(kp):
+        A = boxes[off[k]:off[k + 1]]
+        g = A.copy()
+        g[:, 0] -= 1
+        g[:, 1] -= 1
+        g[:, 2] += 1
+        g[:, 3] += 1
+        p1 = engine.boost_polygon_merge(g)                      # GROW = grow + heal
+        p2 = engine.boost_polygon_operation(A, A[:0], 5, -1)    # SIZE -1
+        outer = engine.boost_polygon_operation(p1, A, 3)        # ~
+        inner = engine.boost_polygon_operation(A, p2, 3)        # ~
+        engine.boost_polygon_operation(outer, A, 2)             # *
+        engine.boost_polygon_operation(outer, inner, 2)         # *
+    plain_s = time.perf_counter() - t0
+    plain = {"value": float(off[kp] / plain_s), "unit": "boxes/s",
+             "sample": "first %d cells (%d boxes), one PerformBoostPolygon* call per operator and cell"
+                       % (kp, int(off[kp]))}
+
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_leg(boxes, off, args.cpu_seconds)
+
+    value = world * nbox / (ms / 1e3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "OP1 deck (GROW 1, SIZE -1, 2x FRAME-NOT, 2x AND, 2x ASSERT_ZERO) + Klee "
+                               "union area on %d cells, lognormal box counts (median %d, sigma 0.92, "
+                               "clip 100..200000), cfg0-style cells" % (args.cells, args.median),
+                   "cells": args.cells, "boxes": nbox, "grid_log2": 16, "seed": args.seed,
+                   "form": "batched: one CUDA-graph replay of persistent kernels per step",
+                   "l2": "inputs (%d MB) larger than L2; no flush" % (nbox * 16 // 2**20)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_tile (scanline Boolean), %d launches/step, %.3f ms/step, "
+                               "algorithmic bytes/step %.3e (pieces read + strips written), peak %s"
+                               % (ntile_per_step, tile_ms_last, bytes_per_step, peak_kind)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": float(nbox / e2e_s), "unit": "boxes/s",
+                "h2d_bytes_per_step": int(nbox * 16 + (args.cells + 1) * 8),
+                "d2h_bytes_per_step": int(args.cells * 7 * 8),
+                "note": "gb_op1_host from pinned host buffers; counts equal the batched run: %s" % e2e_ok},
+        "plain": plain,
+        "gpu_launches": nkern * args.steps,
+        "clocks": clocks,
+        "assert_zero_failures": fails,
+        "parity": parity,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

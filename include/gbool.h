@@ -121,7 +121,8 @@ void gb_clear_status(gb_context* ctx);
 /* Arena marks: layers created after a mark are invalid after releasing it. */
 unsigned long long gb_arena_mark(gb_context* ctx);
 int gb_arena_release(gb_context* ctx, unsigned long long mark);
-/* Output slots per input piece of a Boolean op (default 3). */
+/* Output pool of a Boolean op, in pieces per input piece (default 2; doubled
+ * and retried automatically by the host-synchronous entry points). */
 int gb_set_capacity_factor(gb_context* ctx, int factor);
 /* Per-CTA scratch of the tile kernel in bytes (default 8 MiB). */
 int gb_set_tile_scratch(gb_context* ctx, unsigned long long bytes);
@@ -169,6 +170,39 @@ int gb_canonical_sort(gb_context* ctx, c_box* boxes, long long n);
 /* Convert um to dbu exactly as the interpreter does: int(1000*r), truncating
  * toward zero (controlparser.f90:146,568-576). */
 int32_t gb_um_to_dbu(double r);
+
+/* ---- deck-level execution */
+/* OP1 ring-check chain (op_template.m4:14-22) on all cells of P with amount a
+ * dbu: outs[0..5] = P_1 (GROW a), P_2 (SIZE -a), outer ring (P_1 ~ P),
+ * inner ring (P ~ P_2), ring_and1 (outer * P), ring_intersection
+ * (outer * inner).  Asynchronous; capturable into a CUDA graph. */
+int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs);
+/* The same deck through host buffers: boxes are copied in, the chain runs,
+ * and per cell the six layer counts (counts[ncell*6], may be NULL) and the
+ * union area of P (area[ncell], may be NULL) are copied out.
+ * *assert_failures receives the number of failing ASSERT_ZEROs. */
+int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                long long* area, int* assert_failures);
+
+/* CUDA-graph capture of an operator chain on the context stream.  Every
+ * replay restarts the work arena at the offset it had at gb_graph_begin. */
+typedef struct gb_graph gb_graph;
+int gb_graph_begin(gb_context* ctx);
+int gb_graph_end(gb_context* ctx, gb_graph** out);
+int gb_graph_launch(gb_context* ctx, gb_graph* g);
+long long gb_graph_kernels(gb_graph* g);
+void gb_graph_destroy(gb_graph* g);
+
+/* Profiling: when on, every scanline-kernel launch is bracketed by CUDA
+ * events; gb_profile_read returns their summed time, the launch count and
+ * the algorithmic bytes the kernel read (pieces) and wrote (strips) since
+ * gb_profile(ctx, 1).  on = 2 resets only the byte counters (event pairs
+ * captured in a graph stay valid); on = 0 stops recording. */
+int gb_profile(gb_context* ctx, int on);
+int gb_profile_read(gb_context* ctx, double* ms_total, long long* launches, long long* bytes_in,
+                    long long* bytes_out);
+long long gb_launch_count(gb_context* ctx);
 
 #ifdef __cplusplus
 }

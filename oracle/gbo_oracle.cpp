@@ -366,6 +366,16 @@ void orc_op1(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, in
   *area = s;
 }
 
+// OP1 on every cell of a batched layer, cells in parallel (OpenMP dynamic
+// schedule; the per-cell operators run single-threaded inside).
+void orc_op1_cells(const orc_box* Ab, const int64_t* off, int64_t ncell, int32_t a, int g,
+                   int64_t* counts, int64_t* area) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < ncell; ++k) {
+    orc_op1(Ab + off[k], off[k + 1] - off[k], a, g, counts + 8 * k, area + k);
+  }
+}
+
 void orc_free(void* p) { std::free(p); }
 
 int orc_num_threads(void) {

@@ -68,6 +68,9 @@ void orc_canonical_sort(orc_box* A, int64_t n);
  * merged(poly), unused. */
 void orc_op1(const orc_box* A, int64_t n, int32_t amount, int grid_log2,
              int64_t* counts, int64_t* area);
+/* orc_op1 over ncell cells (off[ncell+1]), cells in parallel: counts[8*k..]. */
+void orc_op1_cells(const orc_box* A, const int64_t* off, int64_t ncell, int32_t amount, int grid_log2,
+                   int64_t* counts, int64_t* area);
 void orc_free(void* p);
 int orc_num_threads(void);
 

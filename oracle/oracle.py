@@ -54,6 +54,8 @@ def lib():
         L.orc_um_to_dbu.restype = i32
         L.orc_op1.argtypes = [P, i64, i32, ctypes.c_int, P, P]
         L.orc_op1.restype = None
+        L.orc_op1_cells.argtypes = [P, P, i64, i32, ctypes.c_int, P, P]
+        L.orc_op1_cells.restype = None
         L.orc_free.argtypes = [P]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -162,6 +164,20 @@ def op1(A, amount=1, grid_log2=16):
     lib().orc_op1(A.ctypes.data, len(A), amount, grid_log2, counts.ctypes.data, area.ctypes.data)
     keys = ["poly_1", "poly_2", "outer_ring", "inner_ring", "ring_and1", "ring_intersection", "merged"]
     return {k: int(counts[i]) for i, k in enumerate(keys)}, int(area[0])
+
+
+def op1_cells(A, off, amount=1, grid_log2=16):
+    """OP1 on every cell (cells in parallel on all OpenMP threads).
+    Returns counts[ncell, 6] (poly_1, poly_2, outer, inner, and1, inter) and
+    the union area per cell."""
+    A = _arr(A)
+    off = np.ascontiguousarray(off, np.int64)
+    ncell = len(off) - 1
+    counts = np.zeros((ncell, 8), np.int64)
+    area = np.zeros(ncell, np.int64)
+    lib().orc_op1_cells(A.ctypes.data, off.ctypes.data, ncell, amount, grid_log2, counts.ctypes.data,
+                        area.ctypes.data)
+    return counts[:, :6], area
 
 
 def canonical(A):

@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -16,32 +17,7 @@
 #define KID_FRAME 50
 #define KID_KEYS 51
 
-struct gb_layer {
-  int slot = -1;
-  DLayer* d = nullptr;  // descriptor in device memory
-  int ncell = 1;
-  int g = 16;
-  int binned = 0;
-  int counted = 0;      // cell_count holds exact strip counts
-  int arena_owned = 0;  // arrays live in the work arena
-  unsigned long long seq = 0;  // creation sequence (arena layers)
-  bool dead = false;
-  void* own_boxes = nullptr;  // raw layers: cudaMalloc'd arrays
-  void* own_coff = nullptr;
-  void* own_cell = nullptr;
-  gb_layer* bin_cache = nullptr;
-  long long nbox_host = 0;
-};
-
-struct gb_context {
-  GbCtx c;
-  std::mutex mu;
-  unsigned long long seq = 0;
-  std::vector<gb_layer*> arena_layers;
-  std::vector<std::pair<unsigned long long, unsigned long long>> marks;  // (device off, seq)
-};
-
-namespace {
+namespace gbi {
 
 int set_err(gb_context* ctx, int code, const char* msg) {
   if (ctx) ctx->c.last_error = msg;
@@ -158,7 +134,8 @@ __global__ void k_fill_frame(const DLayer* P, DLayer* F, int ncell, int t, DStat
   }
 }
 
-__global__ void k_count_tiles(const DLayer* L, long long* per_cell, int ncell) {
+__global__ void k_count_tiles(const DLayer* L, long long* per_cell, int ncell, DStatus* st) {
+  if (st->err || !L->tcount || !L->tbase) return;
   const long long nt = L->ntiles;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nt;
        t += (long long)gridDim.x * blockDim.x) {
@@ -283,7 +260,8 @@ int realloc_scratch(gb_context* ctx, size_t bytes) {
   return GB_OK;
 }
 
-}  // namespace
+}  // namespace gbi
+using namespace gbi;
 
 // ======================================================================= context
 extern "C" int gb_context_create(int device, unsigned long long arena_bytes, gb_context** out) {
@@ -302,8 +280,8 @@ extern "C" int gb_context_create(int device, unsigned long long arena_bytes, gb_
   size_t freeb = 0, totb = 0;
   cudaMemGetInfo(&freeb, &totb);
   if (arena_bytes == 0) {
-    arena_bytes = (unsigned long long)(freeb / 4);
-    const unsigned long long lim = 48ull << 30;
+    arena_bytes = (unsigned long long)(freeb / 2);
+    const unsigned long long lim = 120ull << 30;
     if (arena_bytes > lim) arena_bytes = lim;
   }
   if (cudaMalloc(&c.arena, arena_bytes) != cudaSuccess) return GB_ERR_OOM;
@@ -379,7 +357,7 @@ extern "C" int gb_sync(gb_context* ctx, long long* need) {
   return s.err;
 }
 
-static int sync_where(gb_context* ctx, int* where, long long* need) {
+int sync_where(gb_context* ctx, int* where, long long* need) {
   int e = gb_sync(ctx, need);
   DStatus s = read_status(ctx);
   if (where) *where = s.where;
@@ -514,7 +492,7 @@ extern "C" int gb_layer_count(gb_context* ctx, gb_layer* L, long long* total, lo
     long long* tmp = nullptr;
     cudaMalloc(&tmp, pc.size() * 8);
     cudaMemsetAsync(tmp, 0, pc.size() * 8, c.stream);
-    k_count_tiles<<<c.work_blocks, 256, 0, c.stream>>>(L->d, tmp, L->ncell);
+    k_count_tiles<<<c.work_blocks, 256, 0, c.stream>>>(L->d, tmp, L->ncell, c.st);
     cudaStreamSynchronize(c.stream);
     cudaMemcpy(pc.data(), tmp, pc.size() * 8, cudaMemcpyDeviceToHost);
     cudaFree(tmp);
@@ -572,7 +550,7 @@ extern "C" void gb_layer_free(gb_context* ctx, gb_layer* L) {
 }
 
 // ======================================================================= operators
-static gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode) {
+gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode) {
   GbCtx& c = ctx->c;
   const int g = 16;
   gb_layer* Ab = binned_of(ctx, A, g);
@@ -595,7 +573,7 @@ extern "C" int gb_op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, gb_
   return *out ? GB_OK : set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
 }
 
-static gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge) {
+gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge) {
   const int g = 16;
   gb_layer* R = new_arena_layer(ctx, A->ncell, g);
   if (!R) return nullptr;
@@ -612,7 +590,7 @@ extern "C" int gb_op_grow(gb_context* ctx, gb_layer* A, int32_t E, int32_t N, in
 }
 
 // SIZE(-t): R = P - ((F - P) (+) [-t,t]^2), F = cell bbox grown by t.
-static gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t) {
+gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t) {
   GbCtx& c = ctx->c;
   const int g = 16;
   gb_layer* Pb = binned_of(ctx, P, g);
@@ -653,7 +631,7 @@ extern "C" int gb_op_area(gb_context* ctx, gb_layer* A, long long* area_per_cell
 // Host-synchronous entry points run their device sequence, check the device
 // status, and on a capacity error enlarge the failing resource and run again.
 template <typename F>
-static int run_retry(gb_context* ctx, F&& body) {
+int run_retry(gb_context* ctx, F&& body) {
   int e = GB_OK;
   for (int attempt = 0; attempt < 6; ++attempt) {
     gb_clear_status(ctx);
@@ -671,8 +649,8 @@ static int run_retry(gb_context* ctx, F&& body) {
     if (e != GB_ERR_CAPACITY) break;
     if (where == 20) {  // tile scratch
       if (realloc_scratch(ctx, ctx->c.tile_scr_bytes * 4) != GB_OK) return GB_ERR_OOM;
-    } else if (where == 21) {  // output slots
-      ctx->c.cap_factor *= 4;
+    } else if (where == 21) {  // output pool
+      ctx->c.cap_factor *= 2;
     } else {
       return set_err(ctx, GB_ERR_OOM, "work arena too small for this operation");
     }
@@ -680,6 +658,8 @@ static int run_retry(gb_context* ctx, F&& body) {
   gb_clear_status(ctx);
   return e;
 }
+
+int gb_run_retry(gb_context* ctx, const std::function<int()>& body) { return run_retry(ctx, body); }
 
 // ======================================================================= connectivity
 extern "C" int gb_components(gb_context* ctx, const c_box* boxes, unsigned long long n,

@@ -268,6 +268,7 @@ __global__ void k_alloc_pcs(DLayer* O, int elem_bytes, DStatus* st) {
   if (st->err) return;
   O->pcs = (unsigned long long*)gb_arena_alloc(st, (unsigned long long)(O->npcs + 1) * elem_bytes,
                                                KID_ALLOC);
+  O->nused = O->npcs;
   if (!O->pcs) O->ntiles = 0;
 }
 
@@ -454,33 +455,23 @@ __global__ void k_bool_window(int op, const DLayer* A, const DLayer* B, DLayer* 
   }
 }
 
-// Slot capacity per output tile (written into tcount, scanned into tstart).
-__global__ void k_slotcap(const DLayer* A, const DLayer* B, DLayer* O, int factor, DStatus* st) {
+// Output pool of a Boolean op: factor x (pieces of A + pieces of B) plus a
+// little per tile.  Each tile reserves exactly its strip count from the pool
+// cursor (nused) once it knows it, so no per-tile slack is needed.
+__global__ void k_pool_alloc(const DLayer* A, const DLayer* B, DLayer* O, int factor, DStatus* st) {
   if (st->err) return;
-  const long long nt = O->ntiles;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nt;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int k = gb_find_cell(O->tbase, O->ncell, t);
-    const int4 w = O->win[k];
-    const long long li = t - O->tbase[k];
-    const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
-    long long ta, tb;
-    long long n = 0;
-    if (tile_index_in(A, k, tx, ty, &ta)) n += A->tcount[ta];
-    if (tile_index_in(B, k, tx, ty, &tb)) n += B->tcount[tb];
-    long long cap = n ? n * factor + 32 : 0;
-    if (cap > (1ll << 30)) cap = 1ll << 30;
-    O->tcount[t] = (int)cap;
-  }
+  const long long na = A ? A->nused : 0, nb = B ? B->nused : 0;
+  O->npcs = (na + nb) * factor + 16 * O->ntiles + 64;
+  O->nused = 0;
+  O->pcs = (unsigned long long*)gb_arena_alloc(st, (unsigned long long)O->npcs * 8, KID_ALLOC);
+  if (!O->pcs) O->ntiles = 0;
 }
 
 void gb_launch_bool_setup(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int ncell,
                           int g, int alloc_slots) {
   k_bool_window<<<1, 1024, 0, c.stream>>>(op, A, B, O, ncell, g, c.st);
   if (!alloc_slots) return;
-  k_slotcap<<<c.work_blocks, 256, 0, c.stream>>>(A, B, O, c.cap_factor, c.st);
-  gb_launch_scan_i32(c, &O->tcount, &O->tstart, &O->ntiles, &O->npcs);
-  k_alloc_pcs<<<1, 1, 0, c.stream>>>(O, 8, c.st);
+  k_pool_alloc<<<1, 1, 0, c.stream>>>(A, op == GB_OP_MERGE ? nullptr : B, O, c.cap_factor, c.st);
 }
 
 // ------------------------------------------------------------------ export

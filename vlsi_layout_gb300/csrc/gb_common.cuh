@@ -67,7 +67,8 @@ struct DLayer {
   int* tcount;             // [ntiles]
   unsigned long long* pcs; // packed pieces
   long long ntiles;
-  long long npcs;          // slot capacity of pcs
+  long long npcs;          // capacity of pcs (pieces)
+  long long nused;         // pieces in use (Boolean results reserve per tile from this cursor)
   int4* cbox;              // [ncell] bounding box (raw and binned)
 };
 

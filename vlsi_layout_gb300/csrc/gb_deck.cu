@@ -1,0 +1,198 @@
+// gb_deck.cu -- deck-level execution: the OP1 ring-check chain on device
+// layers, CUDA-graph capture of operator chains, and kernel profiling.
+//
+// OP1 (op_template.m4:14-22, the README ring check):
+//   t1:P_1 = d1:P GROW t1:nothing a a a a
+//   t1:P_2 = d1:P SIZE t1:nothing -a
+//   t1:P_outer_ring = t1:P_1 ~ d1:P
+//   t1:P_inner_ring = d1:P ~ t1:P_2
+//   t1:P_ring_and1 = t1:P_outer_ring * d1:P
+//   t1:P_ring_intersection = t1:P_outer_ring * t1:P_inner_ring
+//   ASSERT_ZERO on the last two
+// Every operator works on all cells of a layer at once, so a batch of
+// independent cells is one launch per kernel, and the whole chain has no
+// host round trip: it can be captured once and replayed as a CUDA graph.
+#include <cstring>
+#include <vector>
+
+#include "gbool.h"
+#include "gb_internal.h"
+
+using namespace gbi;
+
+struct gb_graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  unsigned long long arena_off = 0;
+  long long kernels = 0;
+};
+
+__global__ void k_zero_prof(long long* ctr) {
+  ctr[8] = 0;
+  ctr[9] = 0;
+}
+__global__ void k_arena_to(DStatus* st, unsigned long long off) { st->arena_off = off; }
+
+// on = 1: start a profiling window (event pairs and byte counters reset);
+// on = 2: reset only the byte counters (keeps event pairs captured in a graph);
+// on = 0: stop recording events.
+extern "C" int gb_profile(gb_context* ctx, int on) {
+  if (!ctx) return GB_ERR_ARG;
+  if (on != 2) {
+    ctx->c.prof = on != 0;
+    ctx->c.prof_used = 0;
+  }
+  k_zero_prof<<<1, 1, 0, ctx->c.stream>>>(ctx->c.tile_counter);
+  return GB_OK;
+}
+
+extern "C" int gb_profile_read(gb_context* ctx, double* ms_total, long long* launches,
+                               long long* bytes_in, long long* bytes_out) {
+  if (!ctx) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  cudaStreamSynchronize(c.stream);
+  double ms = 0;
+  long long n = 0;
+  for (size_t i = 0; i + 1 < c.prof_used; i += 2) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, c.prof_ev[i], c.prof_ev[i + 1]) == cudaSuccess) {
+      ms += t;
+      ++n;
+    }
+  }
+  cudaGetLastError();
+  long long ctr[10];
+  cudaMemcpy(ctr, c.tile_counter, sizeof(ctr), cudaMemcpyDeviceToHost);
+  if (ms_total) *ms_total = ms;
+  if (launches) *launches = n;
+  if (bytes_in) *bytes_in = ctr[8];
+  if (bytes_out) *bytes_out = ctr[9];
+  return GB_OK;
+}
+
+extern "C" long long gb_launch_count(gb_context* ctx) { return ctx ? ctx->c.launches : 0; }
+
+extern "C" int gb_graph_begin(gb_context* ctx) {
+  if (!ctx) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  DStatus s = read_status(ctx);
+  ctx->graph_arena_off = s.arena_off;
+  if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return set_err(ctx, GB_ERR_CUDA, "cudaStreamBeginCapture failed");
+  // every replay starts allocating from the same arena offset
+  k_arena_to<<<1, 1, 0, c.stream>>>(c.st, s.arena_off);
+  return GB_OK;
+}
+
+extern "C" int gb_graph_end(gb_context* ctx, gb_graph** out) {
+  if (!ctx || !out) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  gb_graph* G = new gb_graph();
+  G->arena_off = ctx->graph_arena_off;
+  if (cudaStreamEndCapture(c.stream, &G->g) != cudaSuccess) {
+    delete G;
+    cudaGetLastError();
+    return set_err(ctx, GB_ERR_CUDA, "cudaStreamEndCapture failed");
+  }
+  if (cudaGraphInstantiate(&G->ex, G->g, 0) != cudaSuccess) {
+    cudaGraphDestroy(G->g);
+    delete G;
+    cudaGetLastError();
+    return set_err(ctx, GB_ERR_CUDA, "cudaGraphInstantiate failed");
+  }
+  size_t nn = 0;
+  cudaGraphGetNodes(G->g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(G->g, nodes.data(), &nn);
+  for (auto& n : nodes) {
+    cudaGraphNodeType t;
+    cudaGraphNodeGetType(n, &t);
+    if (t == cudaGraphNodeTypeKernel) ++G->kernels;
+  }
+  *out = G;
+  return GB_OK;
+}
+
+extern "C" int gb_graph_launch(gb_context* ctx, gb_graph* G) {
+  if (!ctx || !G) return GB_ERR_ARG;
+  return cudaGraphLaunch(G->ex, ctx->c.stream) == cudaSuccess ? GB_OK
+                                                               : set_err(ctx, GB_ERR_CUDA, "cudaGraphLaunch failed");
+}
+
+extern "C" long long gb_graph_kernels(gb_graph* G) { return G ? G->kernels : 0; }
+
+extern "C" void gb_graph_destroy(gb_graph* G) {
+  if (!G) return;
+  if (G->ex) cudaGraphExecDestroy(G->ex);
+  if (G->g) cudaGraphDestroy(G->g);
+  delete G;
+}
+
+extern "C" int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs) {
+  if (!ctx || !P || !outs || P->dead) return GB_ERR_ARG;
+  gb_layer* p1 = a >= 0 ? op_grow(ctx, P, a, a, a, a, true) : op_erode(ctx, P, -a);
+  gb_layer* p2 = a > 0 ? op_erode(ctx, P, a) : (a == 0 ? op_bool(ctx, GB_OP_MERGE, P, nullptr, 0)
+                                                        : op_grow(ctx, P, -a, -a, -a, -a, true));
+  if (!p1 || !p2) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  gb_layer* outer = op_bool(ctx, GB_OP_NOT, p1, P, 0);
+  gb_layer* inner = op_bool(ctx, GB_OP_NOT, P, p2, 0);
+  if (!outer || !inner) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  gb_layer* and1 = op_bool(ctx, GB_OP_AND, outer, P, 0);
+  gb_layer* inter = op_bool(ctx, GB_OP_AND, outer, inner, 0);
+  if (!and1 || !inter) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  outs[0] = p1; outs[1] = p2; outs[2] = outer; outs[3] = inner; outs[4] = and1; outs[5] = inter;
+  return GB_OK;
+}
+
+__global__ void k_gather_counts(const DLayer* const* L, int nl, int ncell, long long* out,
+                                const DLayer* area_layer, long long* area_out, DStatus* st) {
+  if (st->err) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncell; k += gridDim.x * blockDim.x) {
+    for (int j = 0; j < nl; ++j) out[(long long)k * nl + j] = L[j]->cell_count ? L[j]->cell_count[k] : -1;
+    if (area_out) area_out[k] = area_layer->cell_area ? area_layer->cell_area[k] : -1;
+  }
+}
+
+extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                           const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                           long long* area, int* assert_failures) {
+  if (!ctx || (!boxes && n) || ncell < 1) return GB_ERR_ARG;
+  if (!cell_offsets) ncell = 1;
+  GbCtx& c = ctx->c;
+  gb_layer* P = nullptr;
+  int e = gb_layer_from_host(ctx, boxes, n, cell_offsets, ncell, &P);
+  if (e) return e;
+  long long* dcounts = nullptr;
+  long long* darea = nullptr;
+  DLayer** dl = nullptr;
+  cudaMalloc(&dcounts, (size_t)ncell * 6 * 8);
+  cudaMalloc(&darea, (size_t)ncell * 8);
+  cudaMalloc(&dl, 8 * sizeof(DLayer*));
+  e = gb_run_retry(ctx, [&]() -> int {
+    gb_layer* outs[6];
+    int r = gb_op1(ctx, P, a, outs);
+    if (r) return r;
+    gb_layer* A = op_bool(ctx, GB_OP_MERGE, P, nullptr, 1);
+    if (!A) return GB_ERR_CAPACITY;
+    DLayer* hl[6];
+    for (int j = 0; j < 6; ++j) hl[j] = outs[j]->d;
+    cudaMemcpyAsync(dl, hl, sizeof(hl), cudaMemcpyHostToDevice, c.stream);
+    k_gather_counts<<<(ncell + 255) / 256, 256, 0, c.stream>>>(dl, 6, ncell, dcounts, A->d, darea, c.st);
+    return GB_OK;
+  });
+  std::vector<long long> hc((size_t)ncell * 6), ha(ncell);
+  if (!e) {
+    cudaMemcpy(hc.data(), dcounts, hc.size() * 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(ha.data(), darea, ha.size() * 8, cudaMemcpyDeviceToHost);
+    int fails = 0;
+    for (int k = 0; k < ncell; ++k) fails += (hc[(size_t)k * 6 + 4] > 0) + (hc[(size_t)k * 6 + 5] > 0);
+    if (assert_failures) *assert_failures = fails;
+    if (counts) memcpy(counts, hc.data(), hc.size() * 8);
+    if (area) memcpy(area, ha.data(), ha.size() * 8);
+  }
+  cudaFree(dcounts);
+  cudaFree(darea);
+  cudaFree(dl);
+  gb_layer_free(ctx, P);
+  return e;
+}

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <string>
 #include <vector>
+#include <functional>
+#include <mutex>
 #include "gb_common.cuh"
 
 #define GB_SCAN_BLOCKS 256
@@ -30,9 +32,57 @@ struct GbCtx {
   size_t tile_scr_bytes = 0;         // bytes per CTA
   DLayer* desc = nullptr;            // descriptor pool [GB_NDESC] in device memory
   std::vector<int> desc_free;
-  int cap_factor = 3;                // output slots per input piece of a Boolean op
+  int cap_factor = 2;                // output pool pieces per input piece of a Boolean op
   std::string last_error;
+  // profiling: CUDA events around every tile-kernel launch
+  bool prof = false;
+  std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
+  size_t prof_used = 0;
+  long long launches = 0;            // kernels issued by the engine (host-side count)
 };
+
+struct gb_layer {
+  int slot = -1;
+  DLayer* d = nullptr;  // descriptor in device memory
+  int ncell = 1;
+  int g = 16;
+  int binned = 0;
+  int counted = 0;      // cell_count holds exact strip counts
+  int arena_owned = 0;  // arrays live in the work arena
+  unsigned long long seq = 0;  // creation sequence (arena layers)
+  bool dead = false;
+  void* own_boxes = nullptr;  // raw layers: cudaMalloc'd arrays
+  void* own_coff = nullptr;
+  void* own_cell = nullptr;
+  gb_layer* bin_cache = nullptr;
+  long long nbox_host = 0;
+};
+
+struct gb_context {
+  GbCtx c;
+  std::mutex mu;
+  unsigned long long seq = 0;
+  std::vector<gb_layer*> arena_layers;
+  std::vector<std::pair<unsigned long long, unsigned long long>> marks;  // (device off, seq)
+  unsigned long long graph_arena_off = 0;
+};
+
+
+// host helpers shared by gb_api.cu and gb_deck.cu
+namespace gbi {
+int set_err(gb_context* ctx, int code, const char* msg);
+gb_layer* new_arena_layer(gb_context* ctx, int ncell, int g);
+gb_layer* binned_of(gb_context* ctx, gb_layer* L, int g);
+DStatus read_status(gb_context* ctx);
+DLayer read_desc(gb_context* ctx, gb_layer* L);
+}
+gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode);
+gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge);
+gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t);
+int sync_where(gb_context* ctx, int* where, long long* need);
+// Run a host-synchronous device sequence; on a capacity error enlarge the
+// failing resource (tile scratch, output slots) and run it again.
+int gb_run_retry(gb_context* ctx, const std::function<int()>& body);
 
 // ---- kernels / launchers (gb_bin.cu)
 // Exclusive scan of an int array into int64 starts.  The array pointers are

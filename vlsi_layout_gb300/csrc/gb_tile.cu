@@ -57,6 +57,7 @@ struct TileSmem {
   const unsigned long long* pa;
   const unsigned long long* pb;
   int nA, nB, cell, err;
+  long long obase;
   unsigned long long up, down;  // scratch bump: bytes (low half) / 32-byte records (high half)
   int* Xt;
   int* Yt;
@@ -340,7 +341,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     if (t >= O->ntiles) break;
     const int nA = s.nA, nB = s.nB, P = nA + nB;
     if (P == 0) {
-      if (tid == 0) O->tcount[t] = 0;
+      if (tid == 0) { O->tcount[t] = 0; O->tstart[t] = 0; }
       continue;
     }
     // ---- A: tile ranks
@@ -446,6 +447,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     if (s.err) {
       if (tid == 0) {
         O->tcount[t] = 0;
+        O->tstart[t] = 0;
         gb_set_error(st, GB_ERR_CAPACITY, KID_TILE, (long long)scr * 2);
       }
       continue;
@@ -481,9 +483,17 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       if (q >= 0) s.succ[q] = p;
       else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
     }
+    if (tid == 0) {
+      s.obase = -1;
+      if (mode == 0 && H > 0) {
+        const long long o = (long long)atomicAdd((unsigned long long*)&O->nused, (unsigned long long)H);
+        if (o + H <= O->npcs) s.obase = o;
+        else gb_set_error(st, GB_ERR_CAPACITY, KID_TILE + 1, o + H);
+      }
+    }
     __syncthreads();
-    const long long cap = mode == 0 ? ((t + 1 < O->ntiles ? O->tstart[t + 1] : O->npcs) - O->tstart[t]) : 0;
-    unsigned long long* outp = mode == 0 ? O->pcs + O->tstart[t] : nullptr;
+    const long long obase = s.obase;
+    unsigned long long* outp = obase >= 0 ? O->pcs + obase : nullptr;
     long long area = 0;
     for (int p = tid; p < NP; p += TK_NT) {
       const PieceRec pr = *rec_at(base, scr, p);
@@ -493,15 +503,21 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       const int shi = rec_at(base, scr, q)->shi & 0x3fffffff;
       const int xs = s.Xt[pr.slo], xe = s.Xt[shi], ylo = s.Yt[pr.ylo], yhi = s.Yt[pr.yhi];
       const int pos = s.sbh[pr.sb] + pr.hrank;
-      if (mode == 0 && pos < cap) outp[pos] = gb_pack(xs, ylo, xe, yhi);
+      if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
       area += (long long)(xe - xs) * (long long)(yhi - ylo);
     }
     area = gb_block_sum(area, s.tmp64);
     if (tid == 0) {
-      O->tcount[t] = mode == 0 ? (int)min((long long)H, cap) : H;
-      if (mode == 0 && H > cap) gb_set_error(st, GB_ERR_CAPACITY, KID_TILE + 1, H);
+      if (mode == 0) {
+        O->tcount[t] = obase >= 0 ? H : 0;
+        O->tstart[t] = obase >= 0 ? obase : 0;
+      } else {
+        O->tcount[t] = H;
+      }
       atomicAdd((unsigned long long*)&O->cell_area[s.cell], (unsigned long long)area);
       atomicAdd((unsigned long long*)&O->cell_count[s.cell], (unsigned long long)H);
+      atomicAdd((unsigned long long*)&counter[8], (unsigned long long)P * 8ull);
+      atomicAdd((unsigned long long*)&counter[9], (unsigned long long)(mode == 0 ? H : 0) * 8ull);
     }
   }
 }
@@ -516,6 +532,21 @@ __global__ void k_zero_counter(long long* ctr) { *ctr = 0; }
 
 void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode) {
   k_zero_counter<<<1, 1, 0, c.stream>>>(c.tile_counter);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (c.prof) {
+    if (c.prof_used + 2 > c.prof_ev.size()) {
+      for (int i = 0; i < 64; ++i) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c.prof_ev.push_back(e);
+      }
+    }
+    e0 = c.prof_ev[c.prof_used++];
+    e1 = c.prof_ev[c.prof_used++];
+    cudaEventRecord(e0, c.stream);
+  }
   k_tile<<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode, c.tile_scratch,
                                                         c.tile_scr_bytes, c.tile_counter, c.st);
+  if (c.prof) cudaEventRecord(e1, c.stream);
+  c.launches += 2;
 }

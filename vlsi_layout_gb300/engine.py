@@ -79,6 +79,16 @@ def lib():
         "thrust_sort_boxes_direct": (None, [P, i64]),
         "thrust_sort_boxes_indirect": (None, [P, P, i64]),
         "device_event_sort": (None, [P, i64]),
+        "gb_op1": (ctypes.c_int, [P, P, i32, P]),
+        "gb_op1_host": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P]),
+        "gb_graph_begin": (ctypes.c_int, [P]),
+        "gb_graph_end": (ctypes.c_int, [P, pp]),
+        "gb_graph_launch": (ctypes.c_int, [P, P]),
+        "gb_graph_kernels": (i64, [P]),
+        "gb_graph_destroy": (None, [P]),
+        "gb_profile": (ctypes.c_int, [P, ctypes.c_int]),
+        "gb_profile_read": (ctypes.c_int, [P, P, P, P, P]),
+        "gb_launch_count": (i64, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -210,6 +220,46 @@ class Context:
         perm = np.zeros(len(b), np.int64)
         self._chk(lib().gb_morton_sort(self.h, b.ctypes.data, len(b), 1, keys.ctypes.data, perm.ctypes.data))
         return b, keys, perm
+
+    def op1(self, P, amount):
+        """OP1 deck on layer P; returns the six result layers."""
+        outs = (ctypes.c_void_p * 6)()
+        self._chk(lib().gb_op1(self.h, P.h, amount, outs))
+        return [Layer(self, ctypes.c_void_p(outs[i]), P.ncell) for i in range(6)]
+
+    def op1_host(self, boxes_ptr, n, offsets, amount):
+        """OP1 deck through host buffers (boxes_ptr: address of n int32x4
+        boxes, e.g. pinned memory).  Returns (counts[ncell,6], area[ncell],
+        assert_failures)."""
+        off = np.ascontiguousarray(offsets, np.int64)
+        ncell = len(off) - 1
+        counts = np.zeros((ncell, 6), np.int64)
+        area = np.zeros(ncell, np.int64)
+        fails = ctypes.c_int()
+        self._chk(lib().gb_op1_host(self.h, ctypes.c_void_p(boxes_ptr), n, off.ctypes.data, ncell, amount,
+                                    counts.ctypes.data, area.ctypes.data, ctypes.byref(fails)))
+        return counts, area, fails.value
+
+    def graph_begin(self):
+        self._chk(lib().gb_graph_begin(self.h))
+
+    def graph_end(self):
+        g = ctypes.c_void_p()
+        self._chk(lib().gb_graph_end(self.h, ctypes.byref(g)))
+        return g
+
+    def graph_launch(self, g):
+        self._chk(lib().gb_graph_launch(self.h, g))
+
+    def profile(self, on):
+        self._chk(lib().gb_profile(self.h, 1 if on else 0))
+
+    def profile_read(self):
+        ms = ctypes.c_double()
+        n, bi, bo = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._chk(lib().gb_profile_read(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(bi),
+                                        ctypes.byref(bo)))
+        return ms.value, n.value, bi.value, bo.value
 
     def canonical_sort(self, boxes):
         b = _boxes(boxes).copy()
