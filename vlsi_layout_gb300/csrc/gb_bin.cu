@@ -269,6 +269,7 @@ __global__ void k_alloc_pcs(DLayer* O, int elem_bytes, DStatus* st) {
   O->pcs = (unsigned long long*)gb_arena_alloc(st, (unsigned long long)(O->npcs + 1) * elem_bytes,
                                                KID_ALLOC);
   O->nused = O->npcs;
+  O->ntot = O->npcs;
   if (!O->pcs) O->ntiles = 0;
 }
 
@@ -457,12 +458,15 @@ __global__ void k_bool_window(int op, const DLayer* A, const DLayer* B, DLayer* 
 
 // Output pool of a Boolean op: factor x (pieces of A + pieces of B) plus a
 // little per tile.  Each tile reserves exactly its strip count from the pool
-// cursor (nused) once it knows it, so no per-tile slack is needed.
+// cursor (nused) once it knows it, so no per-tile slack is needed; a tile
+// that no longer fits takes its slots from the arena directly (atomically),
+// at an offset relative to the pool base.
 __global__ void k_pool_alloc(const DLayer* A, const DLayer* B, DLayer* O, int factor, DStatus* st) {
   if (st->err) return;
-  const long long na = A ? A->nused : 0, nb = B ? B->nused : 0;
+  const long long na = A ? A->ntot : 0, nb = B ? B->ntot : 0;
   O->npcs = (na + nb) * factor + 16 * O->ntiles + 64;
   O->nused = 0;
+  O->ntot = 0;
   O->pcs = (unsigned long long*)gb_arena_alloc(st, (unsigned long long)O->npcs * 8, KID_ALLOC);
   if (!O->pcs) O->ntiles = 0;
 }

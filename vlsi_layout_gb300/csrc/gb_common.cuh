@@ -68,7 +68,8 @@ struct DLayer {
   unsigned long long* pcs; // packed pieces
   long long ntiles;
   long long npcs;          // capacity of pcs (pieces)
-  long long nused;         // pieces in use (Boolean results reserve per tile from this cursor)
+  long long nused;         // pool cursor (Boolean results reserve per tile from it)
+  long long ntot;          // pieces held by the layer
   int4* cbox;              // [ncell] bounding box (raw and binned)
 };
 
@@ -104,6 +105,19 @@ __device__ inline void* gb_arena_alloc(DStatus* st, unsigned long long bytes, in
   }
   st->arena_off = end;
   if (end > st->arena_high) st->arena_high = end;
+  return st->arena_base + off;
+}
+
+// Concurrent bump allocation (many CTAs at once).  Setup kernels use the
+// single-thread form above; both never run at the same time on one stream.
+__device__ inline void* gb_arena_alloc_atomic(DStatus* st, unsigned long long bytes, int where) {
+  const unsigned long long sz = (bytes + 255ull) & ~255ull;
+  const unsigned long long off = atomicAdd(&st->arena_off, sz);
+  if (off + sz > st->arena_cap) {
+    gb_set_error(st, GB_ERR_CAPACITY, where, (long long)(off + sz));
+    return nullptr;
+  }
+  atomicMax(&st->arena_high, off + sz);
   return st->arena_base + off;
 }
 

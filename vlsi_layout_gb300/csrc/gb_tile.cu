@@ -486,9 +486,15 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     if (tid == 0) {
       s.obase = -1;
       if (mode == 0 && H > 0) {
+        atomicAdd((unsigned long long*)&O->ntot, (unsigned long long)H);
         const long long o = (long long)atomicAdd((unsigned long long*)&O->nused, (unsigned long long)H);
-        if (o + H <= O->npcs) s.obase = o;
-        else gb_set_error(st, GB_ERR_CAPACITY, KID_TILE + 1, o + H);
+        if (o + H <= O->npcs) {
+          s.obase = o;
+        } else {
+          unsigned long long* p =
+              (unsigned long long*)gb_arena_alloc_atomic(st, (unsigned long long)H * 8ull, KID_TILE + 1);
+          if (p) s.obase = (long long)(p - O->pcs);
+        }
       }
     }
     __syncthreads();
