@@ -70,6 +70,25 @@ extern "C" int gb_profile_read(gb_context* ctx, double* ms_total, long long* lau
   return GB_OK;
 }
 
+// Per-phase cycle counters of the scanline kernel (diagnostics): on != 0
+// enables them; gb_tile_timing_read returns [cycA, cycB, cycC, cycD, tiles,
+// pieces, sub-bands, strip pieces] summed over CTAs since enabling.
+__global__ void k_zero_timing(long long* ctr) {
+  for (int i = 16; i < 32; ++i) ctr[i] = 0;
+}
+extern "C" int gb_tile_timing(gb_context* ctx, int on) {
+  if (!ctx) return GB_ERR_ARG;
+  ctx->c.timing = on != 0;
+  k_zero_timing<<<1, 1, 0, ctx->c.stream>>>(ctx->c.tile_counter);
+  return GB_OK;
+}
+extern "C" int gb_tile_timing_read(gb_context* ctx, long long* out8) {
+  if (!ctx || !out8) return GB_ERR_ARG;
+  cudaStreamSynchronize(ctx->c.stream);
+  cudaMemcpy(out8, ctx->c.tile_counter + 16, 16 * sizeof(long long), cudaMemcpyDeviceToHost);
+  return GB_OK;
+}
+
 extern "C" long long gb_launch_count(gb_context* ctx) { return ctx ? ctx->c.launches : 0; }
 
 extern "C" int gb_graph_begin(gb_context* ctx) {

@@ -38,6 +38,8 @@ struct GbCtx {
   bool prof = false;
   std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
   size_t prof_used = 0;
+  unsigned prof_flags = 0;
+  bool timing = false;               // per-phase clock64 counters in the tile kernel
   long long launches = 0;            // kernels issued by the engine (host-side count)
 };
 

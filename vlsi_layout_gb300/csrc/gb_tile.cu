@@ -35,13 +35,14 @@
 #include "gb_internal.h"
 #include "gb_scan.cuh"
 
-#define TK_NW 12
+#define TK_NW 8
 #define TK_NT (TK_NW * 32)
 #define TK_WMAX 2049
 #define TK_NSBMAX 1042
-#define TK_LBW 256
-#define TK_LVN 512
-#define TK_LCN 256
+#define TK_LBW 128
+#define TK_LVN 256
+#define TK_LCN 128
+#define TK_MW 64
 #define KID_TILE 20
 
 struct TileSmem {
@@ -52,6 +53,9 @@ struct TileSmem {
   int lv[TK_NW][TK_LVN];
   unsigned long long ca[TK_NW][TK_LCN];
   unsigned long long cb[TK_NW][TK_LCN];
+  int4 mc[TK_NW][TK_MW];                 // member cache: slab range (owner in bit 31), y ranks
+  unsigned srow[TK_NW][64][TK_LCN / 32]; // run starts, row-major (transposed), for start lookups
+  int sbnext;                            // next sub-band to hand to a warp
   long long tmp64[33];
   long long tile;
   const unsigned long long* pa;
@@ -106,8 +110,10 @@ __device__ __forceinline__ PieceRec* rec_at(char* base, unsigned long long scr, 
 }
 
 __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int nA, char* base,
-                             unsigned long long scr) {
+                             unsigned long long scr, long long* tctr) {
   const int lane = gb_lane(), wid = gb_warp();
+  long long q0 = tctr ? clock64() : 0;
+#define TSTEP(k) if (tctr && lane == 0) { const long long q1 = clock64(); atomicAdd((unsigned long long*)&tctr[k], (unsigned long long)(q1 - q0)); q0 = q1; }
   const unsigned long long half = scr >> 1;
   const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
   const int m = end - beg;
@@ -119,10 +125,13 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int nwy = ((Ny - 1) >> 5) + 1;
   unsigned* lb = nwy <= TK_LBW ? s.lb[wid] : s.biglb + (size_t)wid * 2 * nwy;
   unsigned* lp = nwy <= TK_LBW ? s.lp[wid] : lb + nwy;
+  const bool cache = m <= TK_MW;
   for (int w = lane; w < nwy; w += 32) lb[w] = 0;
   __syncwarp();
   for (int j = lane; j < m; j += 32) {
-    const int4 r = s.rk[s.mem[beg + j]];
+    const int i = s.mem[beg + j];
+    const int4 r = s.rk[i];
+    if (cache) s.mc[wid][j] = make_int4(r.x | ((i >= nA) ? (int)0x80000000 : 0), r.y, r.z, r.w);
     atomicOr(&lb[r.z >> 5], 1u << (r.z & 31));
     atomicOr(&lb[r.w >> 5], 1u << (r.w & 31));
   }
@@ -138,6 +147,11 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     nl = tot;
   }
   const int L = nl - 1;
+  TSTEP(0)
+  if (tctr && lane == 0) {
+    atomicAdd((unsigned long long*)&tctr[6], (unsigned long long)m);
+    atomicAdd((unsigned long long*)&tctr[7], (unsigned long long)L);
+  }
   int* lv = s.lv[wid];
   unsigned long long* ca = s.ca[wid];
   unsigned long long* cb = s.cb[wid];
@@ -165,23 +179,92 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       }
     }
   }
-  for (int c = lane; c < L; c += 32) { ca[c] = 0; cb[c] = 0; }
+  // ---- rasterise: one member per lane; each column word is updated as two
+  // 32-bit halves with native shared-memory atomicOr
+  const int per = (L + 31) >> 5, c0 = min(L, lane * per), c1e = min(L, c0 + per);
+  for (int c = c0; c < c1e; ++c) { ca[c] = 0; cb[c] = 0; }
   __syncwarp();
-  for (int j = lane; j < m; j += 32) {
-    const int i = s.mem[beg + j];
-    const int4 r = s.rk[i];
-    const int lc1 = bm_rank(lb, lp, r.z), lc2 = bm_rank(lb, lp, r.w);
-    const int lo = max(r.x - rowbase, 0), hi = min(r.y - rowbase, 64);
-    const unsigned long long mask = (hi >= 64 ? ~0ull : ((1ull << hi) - 1ull)) & (~0ull << lo);
-    unsigned long long* col = i < nA ? ca : cb;
-    for (int c = lc1; c < lc2; ++c) atomicOr(&col[c], mask);
+  // 32 members at a time: the (member, column) pairs of the group are spread
+  // evenly over the lanes (a warp scan of the spans, then a shuffle search for
+  // the member of each pair), so one long member does not serialise a lane.
+  for (int jb = 0; jb < m; jb += 32) {
+    const int j = jb + lane;
+    int lc1 = 0, span = 0, own = 0;
+    unsigned long long mk = 0;
+    if (j < m) {
+      int4 r;
+      if (cache) {
+        r = s.mc[wid][j];
+        own = (r.x >> 31) & 1;
+        r.x &= 0x7fffffff;
+      } else {
+        const int i = s.mem[beg + j];
+        r = s.rk[i];
+        own = i >= nA;
+      }
+      const int lo = max(r.x - rowbase, 0), hi = min(r.y - rowbase, 64);
+      mk = (hi >= 64 ? ~0ull : ((1ull << hi) - 1ull)) & (~0ull << lo);
+      lc1 = bm_rank(lb, lp, r.z);
+      span = bm_rank(lb, lp, r.w) - lc1;
+    }
+    const int incl = gb_warp_incl(span);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int k0 = 0; k0 < total; k0 += 32) {  // warp-uniform trip count
+      const int k = k0 + lane;
+      // owner lane: the first lane whose inclusive prefix exceeds k
+      int o = 0;
+#pragma unroll
+      for (int st2 = 16; st2 > 0; st2 >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, incl, o + st2 - 1);
+        if (v <= k) o += st2;
+      }
+      const int ex_o = __shfl_sync(0xffffffffu, incl - span, o);
+      const int c1_o = __shfl_sync(0xffffffffu, lc1, o);
+      const int own_o = __shfl_sync(0xffffffffu, own, o);
+      const unsigned long long mk_o = __shfl_sync(0xffffffffu, mk, o);
+      if (k < total) {
+        unsigned* col = (unsigned*)(own_o ? cb : ca);
+        const int c = c1_o + (k - ex_o);
+        if ((unsigned)mk_o) atomicOr(&col[2 * c], (unsigned)mk_o);
+        if ((unsigned)(mk_o >> 32)) atomicOr(&col[2 * c + 1], (unsigned)(mk_o >> 32));
+      }
+    }
   }
   __syncwarp();
-  for (int c = lane; c < L; c += 32) ca[c] = gb_pred(op, ca[c], cb[c]);
+  for (int c = c0; c < c1e; ++c) ca[c] = gb_pred(op, ca[c], cb[c]);
   __syncwarp();
+  // ---- run starts S_c = R_c & ~R_{c-1}, transposed to one column bitmap per row
+  const bool tr = L <= TK_LCN;
+  if (tr) {
+    const int nb = (L + 31) >> 5;
+    for (int b = 0; b < nb; ++b) {
+      const int c = (b << 5) + lane;
+      const unsigned long long Rc = c < L ? ca[c] : 0ull;
+      const unsigned long long Rm = (c >= 1 && c - 1 < L) ? ca[c - 1] : 0ull;
+      const unsigned long long S = Rc & ~Rm;
+      unsigned lo = (unsigned)S, hi = (unsigned)(S >> 32);
+#pragma unroll
+      for (int j = 16; j > 0; j >>= 1) {
+        const unsigned m0 = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu
+                          : j == 2 ? 0x33333333u : 0x55555555u;
+        const unsigned tlo = __shfl_xor_sync(0xffffffffu, lo, j);
+        const unsigned thi = __shfl_xor_sync(0xffffffffu, hi, j);
+        if (lane & j) {
+          lo = ((tlo & ~m0) >> j) | (lo & ~m0);
+          hi = ((thi & ~m0) >> j) | (hi & ~m0);
+        } else {
+          lo = (lo & m0) | ((tlo & m0) << j);
+          hi = (hi & m0) | ((thi & m0) << j);
+        }
+      }
+      s.srow[wid][lane][b] = lo;
+      s.srow[wid][32 + lane][b] = hi;
+    }
+    __syncwarp();
+  }
+  TSTEP(1)
 
   // ---- forward segmented OR-scan over the columns (bit-parallel over rows)
-  const int per = (L + 31) >> 5, c0 = min(L, lane * per), c1e = min(L, c0 + per);
   auto R = [&](int c) -> unsigned long long { return (c < 0 || c >= L) ? 0ull : ca[c]; };
   unsigned long long FA = 0ull, FB = ~0ull;
   {
@@ -206,6 +289,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   unsigned long long Fin = __shfl_up_sync(0xffffffffu, IA, 1);
   if (lane == 0) Fin = 0ull;
   const bool last_sb = (sb == nsb - 1);
+  TSTEP(2)
 
   // ---- count pieces / opens / heads
   int np = 0, no = 0, nh = 0;
@@ -246,6 +330,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   obase = __shfl_sync(0xffffffffu, obase, 0);
   if (pbase < 0) return;
   int* olist = (int*)(base + obase);
+  TSTEP(3)
 
   // ---- write pieces
   {
@@ -266,10 +351,17 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         const unsigned long long above = (r >= 63) ? 0ull : ((Z | ~Ec) & (~0ull << (r + 1)));
         const int rend = above ? (__ffsll((long long)above) - 1) : 64;
         int cs = c;
-        while (cs > 0) {
-          const unsigned long long S2 = ca[cs] & ~ca[cs - 1];
-          if ((S2 >> r) & 1ull) break;
-          --cs;
+        if (tr) {
+          int b = c >> 5;
+          unsigned mk = s.srow[wid][r][b] & (0xFFFFFFFFu >> (31 - (c & 31)));
+          while (!mk && b > 0) mk = s.srow[wid][r][--b];
+          cs = (b << 5) + 31 - __clz(mk);
+        } else {
+          while (cs > 0) {
+            const unsigned long long S2 = ca[cs] & ~ca[cs - 1];
+            if ((S2 >> r) & 1ull) break;
+            --cs;
+          }
         }
         const int cont = (sb > 0) && (r == 1) && !((Chg >> 1) & 1ull);
         const int open = (rend == 64) && !last_sb;
@@ -290,13 +382,15 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       Rm1 = Rc;
     }
   }
+  TSTEP(4)
   if (lane == 0) {
     s.sbinfo[sb] = make_int4(pbase, totP, (int)obase, totO);
     s.sbh[sb] = totH;
   }
+#undef TSTEP
 }
 
-__global__ void __launch_bounds__(TK_NT, 1)
+__global__ void __launch_bounds__(TK_NT, 2)
 k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, char* scratch,
        unsigned long long scr, long long* counter, DStatus* st) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -305,6 +399,9 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
   char* base = scratch + (size_t)blockIdx.x * scr;
   const unsigned long long half = scr >> 1;
   const int W = ((1 << g) >> 5) + 1;
+  const bool timing = (mode & 4) != 0;
+  mode &= 3;
+  long long tA = 0, tB = 0, tC = 0, tD = 0, t0 = 0;
   for (;;) {
     __syncthreads();
     if (tid == 0) {
@@ -344,6 +441,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       if (tid == 0) { O->tcount[t] = 0; O->tstart[t] = 0; }
       continue;
     }
+    if (timing) t0 = clock64();
     // ---- A: tile ranks
     for (int w = tid; w < W; w += TK_NT) { s.xb[w] = 0; s.yb[w] = 0; }
     __syncthreads();
@@ -390,6 +488,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     const int nslab = Nx - 1;
     const int nsb = (nslab + 62) / 63;
+    if (timing) { __syncthreads(); const long long t1 = clock64(); tA += t1 - t0; t0 = t1; }
     // ---- B: sub-band membership (counting sort in shared memory)
     for (int i = tid; i <= nsb; i += TK_NT) s.sbc[i] = 0;
     __syncthreads();
@@ -436,10 +535,21 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
     }
     __syncthreads();
-    // ---- C: one warp per sub-band
-    if (!s.err)
-      for (int sb = gb_warp(); sb < nsb; sb += TK_NW) tile_subband(s, op, sb, nsb, Ny, nA, base, scr);
+    if (timing) { const long long t1 = clock64(); tB += t1 - t0; t0 = t1; }
+    // ---- C: one warp per sub-band, handed out dynamically
+    if (tid == 0) s.sbnext = 0;
     __syncthreads();
+    if (!s.err) {
+      for (;;) {
+        int sb = 0;
+        if (gb_lane() == 0) sb = atomicAdd(&s.sbnext, 1);
+        sb = __shfl_sync(0xffffffffu, sb, 0);
+        if (sb >= nsb) break;
+        tile_subband(s, op, sb, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
+      }
+    }
+    __syncthreads();
+    if (timing) { const long long t1 = clock64(); tC += t1 - t0; t0 = t1; }
     // ---- D: stitch and emit
     const int NP = (int)s.down;
     if (tid == 0 && !s.err) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
@@ -522,16 +632,32 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       atomicAdd((unsigned long long*)&O->cell_area[s.cell], (unsigned long long)area);
       atomicAdd((unsigned long long*)&O->cell_count[s.cell], (unsigned long long)H);
+      if (timing) {
+        const long long t1 = clock64();
+        tD += t1 - t0;
+        atomicAdd((unsigned long long*)&counter[20], 1ull);
+        atomicAdd((unsigned long long*)&counter[21], (unsigned long long)P);
+        atomicAdd((unsigned long long*)&counter[22], (unsigned long long)nsb);
+        atomicAdd((unsigned long long*)&counter[23], (unsigned long long)NP);
+      }
       atomicAdd((unsigned long long*)&counter[8], (unsigned long long)P * 8ull);
       atomicAdd((unsigned long long*)&counter[9], (unsigned long long)(mode == 0 ? H : 0) * 8ull);
     }
+  }
+  if (timing && threadIdx.x == 0) {
+    atomicAdd((unsigned long long*)&counter[16], (unsigned long long)tA);
+    atomicAdd((unsigned long long*)&counter[17], (unsigned long long)tB);
+    atomicAdd((unsigned long long*)&counter[18], (unsigned long long)tC);
+    atomicAdd((unsigned long long*)&counter[19], (unsigned long long)tD);
   }
 }
 
 void gb_tile_setup(GbCtx& c) {
   c.tile_smem = sizeof(TileSmem);
   cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.tile_smem);
-  c.tile_blocks = c.nsm;
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile, TK_NT, c.tile_smem);
+  c.tile_blocks = c.nsm * (per_sm > 0 ? per_sm : 1);
 }
 
 __global__ void k_zero_counter(long long* ctr) { *ctr = 0; }
@@ -549,10 +675,14 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
     }
     e0 = c.prof_ev[c.prof_used++];
     e1 = c.prof_ev[c.prof_used++];
-    cudaEventRecord(e0, c.stream);
+    // inside a stream capture only an external record becomes a real event node
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(c.stream, &cs);
+    c.prof_flags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0;
+    cudaEventRecordWithFlags(e0, c.stream, c.prof_flags);
   }
-  k_tile<<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode, c.tile_scratch,
+  k_tile<<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode | (c.timing ? 4 : 0), c.tile_scratch,
                                                         c.tile_scr_bytes, c.tile_counter, c.st);
-  if (c.prof) cudaEventRecord(e1, c.stream);
+  if (c.prof) cudaEventRecordWithFlags(e1, c.stream, c.prof_flags);
   c.launches += 2;
 }
