@@ -204,7 +204,7 @@ int gb_profile_read(gb_context* ctx, double* ms_total, long long* launches, long
                     long long* bytes_out);
 long long gb_launch_count(gb_context* ctx);
 /* Diagnostics: per-phase cycle counters of the scanline kernel.  out8 (16
- * entries) gets cycles of phases A (ranks), B (sub-band lists), C (sub-band
+ * entries, 24 with the raster sub-steps) gets cycles of phases A (ranks), B (sub-band lists), C (sub-band
  * sweeps), D (stitch/emit) summed over CTAs; tiles, pieces, sub-bands, strip
  * pieces; then per-warp cycles of the sub-band steps (compress, rasterise,
  * scan, count, write), members and columns, since gb_tile_timing(ctx, 1). */

@@ -74,7 +74,7 @@ extern "C" int gb_profile_read(gb_context* ctx, double* ms_total, long long* lau
 // enables them; gb_tile_timing_read returns [cycA, cycB, cycC, cycD, tiles,
 // pieces, sub-bands, strip pieces] summed over CTAs since enabling.
 __global__ void k_zero_timing(long long* ctr) {
-  for (int i = 16; i < 32; ++i) ctr[i] = 0;
+  for (int i = 16; i < 40; ++i) ctr[i] = 0;
 }
 extern "C" int gb_tile_timing(gb_context* ctx, int on) {
   if (!ctx) return GB_ERR_ARG;
@@ -85,7 +85,7 @@ extern "C" int gb_tile_timing(gb_context* ctx, int on) {
 extern "C" int gb_tile_timing_read(gb_context* ctx, long long* out8) {
   if (!ctx || !out8) return GB_ERR_ARG;
   cudaStreamSynchronize(ctx->c.stream);
-  cudaMemcpy(out8, ctx->c.tile_counter + 16, 16 * sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaMemcpy(out8, ctx->c.tile_counter + 16, 24 * sizeof(long long), cudaMemcpyDeviceToHost);
   return GB_OK;
 }
 

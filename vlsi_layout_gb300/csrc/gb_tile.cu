@@ -32,6 +32,9 @@
 //     Strips are written in (sub-band, column, row) order, so the output of a
 //     tile is deterministic.
 // No piece ever waits on another CTA: there is no spin-wait in this kernel.
+#include <cstdio>
+#include <mutex>
+
 #include "gb_internal.h"
 #include "gb_scan.cuh"
 
@@ -45,16 +48,42 @@
 #define TK_MW 64
 #define KID_TILE 20
 
+// A strip piece of one sub-band, 16 bytes, stored downward from the top of
+// the CTA scratch.  x: y1 rank | cont << 30 | open << 31; y: y2 rank | low 15
+// bits of the head rank << 17; z: first x-slab | high bits of the head rank
+// << 17; w: end x-slab.  Ranks and slabs are below 2^17.
+struct PieceRec {
+  int x, y, z, w;
+};
+__device__ __forceinline__ int pr_ylo(const PieceRec& p) { return p.x & 0x1ffff; }
+__device__ __forceinline__ int pr_yhi(const PieceRec& p) { return p.y & 0x1ffff; }
+__device__ __forceinline__ int pr_slo(const PieceRec& p) { return p.z & 0x1ffff; }
+__device__ __forceinline__ int pr_shi(const PieceRec& p) { return p.w; }
+__device__ __forceinline__ bool pr_cont(const PieceRec& p) { return (p.x >> 30) & 1; }
+__device__ __forceinline__ int pr_hrank(const PieceRec& p) {
+  return (int)(((unsigned)p.y >> 17) | (((unsigned)p.z >> 17) << 15));
+}
+
 struct TileSmem {
-  unsigned xb[TK_WMAX], xp[TK_WMAX], yb[TK_WMAX], yp[TK_WMAX];
+  union {  // phases A-B: value bitmaps and their prefix popcounts; phase D: x / y value tables
+    struct {
+      unsigned xb[TK_WMAX], xp[TK_WMAX], yb[TK_WMAX], yp[TK_WMAX];
+    };
+    int xyv[4 * TK_WMAX];
+  };
   int sbc[TK_NSBMAX + 2];
-  unsigned lb[TK_NW][TK_LBW];
-  unsigned lp[TK_NW][TK_LBW];
-  int lv[TK_NW][TK_LVN];
-  unsigned long long ca[TK_NW][TK_LCN];
-  unsigned long long cb[TK_NW][TK_LCN];
-  int4 mc[TK_NW][TK_MW];                 // member cache: slab range (owner in bit 31), y ranks
-  unsigned srow[TK_NW][64][TK_LCN / 32]; // run starts, row-major (transposed), for start lookups
+  union {  // phase C: per-warp sweep buffers; phase D: piece records and chain links
+    struct {
+      unsigned lb[TK_NW][TK_LBW];
+      unsigned lp[TK_NW][TK_LBW];
+      int lv[TK_NW][TK_LVN];
+      unsigned long long ca[TK_NW][TK_LCN];
+      unsigned long long cb[TK_NW][TK_LCN];
+      int4 mc[TK_NW][TK_MW];                  // member cache: slab range (owner bit 31), y ranks
+      unsigned srow[TK_NW][64][TK_LCN / 32];  // run starts, row-major (transposed)
+    };
+    unsigned char dbuf[1];
+  };
   int sbnext;                            // next sub-band to hand to a warp
   long long tmp64[33];
   long long tile;
@@ -66,9 +95,10 @@ struct TileSmem {
   int* Xt;
   int* Yt;
   int4* rk;
-  int* mem;
+  int4* mem;  // member records: x1-slab | owner<<31, x2-slab, y1 rank, y2 rank
   int4* sbinfo;  // per sub-band: piece base, piece count, open-list byte offset, open count
   int* sbh;      // heads per sub-band, then their exclusive scan
+  int* sbct;     // continuation pieces per sub-band
   unsigned* biglb;
   int* succ;
 };
@@ -100,13 +130,8 @@ __device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long lo
   return base + off;
 }
 
-struct PieceRec {  // 32 bytes, stored downward from the top of the scratch
-  int ylo, yhi, slo, shi;  // y ranks, x-slab range; shi carries flags (bit30 cont, bit31 open)
-  int hrank, sb, pad0, pad1;
-};
-
 __device__ __forceinline__ PieceRec* rec_at(char* base, unsigned long long scr, int p) {
-  return reinterpret_cast<PieceRec*>(base + scr - 32ull * (unsigned long long)(p + 1));
+  return reinterpret_cast<PieceRec*>(base + scr - 16ull * (unsigned long long)(p + 1));
 }
 
 __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int nA, char* base,
@@ -118,7 +143,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
   const int m = end - beg;
   if (m == 0) {
-    if (lane == 0) { s.sbinfo[sb] = make_int4(0, 0, 0, 0); s.sbh[sb] = 0; }
+    if (lane == 0) { s.sbinfo[sb] = make_int4(0, 0, 0, 0); s.sbh[sb] = 0; s.sbct[sb] = 0; }
     return;
   }
   const int rowbase = 63 * sb - 1;
@@ -129,9 +154,8 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   for (int w = lane; w < nwy; w += 32) lb[w] = 0;
   __syncwarp();
   for (int j = lane; j < m; j += 32) {
-    const int i = s.mem[beg + j];
-    const int4 r = s.rk[i];
-    if (cache) s.mc[wid][j] = make_int4(r.x | ((i >= nA) ? (int)0x80000000 : 0), r.y, r.z, r.w);
+    const int4 r = s.mem[beg + j];
+    if (cache) s.mc[wid][j] = r;
     atomicOr(&lb[r.z >> 5], 1u << (r.z & 31));
     atomicOr(&lb[r.w >> 5], 1u << (r.w & 31));
   }
@@ -187,52 +211,67 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   // 32 members at a time: the (member, column) pairs of the group are spread
   // evenly over the lanes (a warp scan of the spans, then a shuffle search for
   // the member of each pair), so one long member does not serialise a lane.
+  long long qa = tctr ? clock64() : 0, qsetup = 0, qpaint = 0;
   for (int jb = 0; jb < m; jb += 32) {
     const int j = jb + lane;
     int lc1 = 0, span = 0, own = 0;
     unsigned long long mk = 0;
     if (j < m) {
-      int4 r;
-      if (cache) {
-        r = s.mc[wid][j];
-        own = (r.x >> 31) & 1;
-        r.x &= 0x7fffffff;
-      } else {
-        const int i = s.mem[beg + j];
-        r = s.rk[i];
-        own = i >= nA;
-      }
+      int4 r = cache ? s.mc[wid][j] : s.mem[beg + j];
+      own = (r.x >> 31) & 1;
+      r.x &= 0x7fffffff;
       const int lo = max(r.x - rowbase, 0), hi = min(r.y - rowbase, 64);
       mk = (hi >= 64 ? ~0ull : ((1ull << hi) - 1ull)) & (~0ull << lo);
       lc1 = bm_rank(lb, lp, r.z);
       span = bm_rank(lb, lp, r.w) - lc1;
     }
-    const int incl = gb_warp_incl(span);
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (int k0 = 0; k0 < total; k0 += 32) {  // warp-uniform trip count
-      const int k = k0 + lane;
-      // owner lane: the first lane whose inclusive prefix exceeds k
-      int o = 0;
-#pragma unroll
-      for (int st2 = 16; st2 > 0; st2 >>= 1) {
-        const int v = __shfl_sync(0xffffffffu, incl, o + st2 - 1);
-        if (v <= k) o += st2;
-      }
-      const int ex_o = __shfl_sync(0xffffffffu, incl - span, o);
-      const int c1_o = __shfl_sync(0xffffffffu, lc1, o);
-      const int own_o = __shfl_sync(0xffffffffu, own, o);
-      const unsigned long long mk_o = __shfl_sync(0xffffffffu, mk, o);
-      if (k < total) {
-        unsigned* col = (unsigned*)(own_o ? cb : ca);
-        const int c = c1_o + (k - ex_o);
-        if ((unsigned)mk_o) atomicOr(&col[2 * c], (unsigned)mk_o);
-        if ((unsigned)(mk_o >> 32)) atomicOr(&col[2 * c + 1], (unsigned)(mk_o >> 32));
+    // direct: the first 4 columns of every member on its own lane
+    {
+      unsigned* col = (unsigned*)(own ? cb : ca);
+      const unsigned mlo = (unsigned)mk, mhi = (unsigned)(mk >> 32);
+      const int d = min(span, 4);
+      for (int c = lc1; c < lc1 + d; ++c) {
+        if (mlo) atomicOr(&col[2 * c], mlo);
+        if (mhi) atomicOr(&col[2 * c + 1], mhi);
       }
     }
+    if (tctr) { const long long qb = clock64(); qsetup += qb - qa; qa = qb; }
+    // remainder of long members: (member, column) pairs spread over the lanes
+    const int rest = max(span - 4, 0);
+    if (__any_sync(0xffffffffu, rest > 0)) {
+      const int incl = gb_warp_incl(rest);
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      if (tctr && lane == 0) atomicAdd((unsigned long long*)&tctr[12], (unsigned long long)total);
+      for (int k0 = 0; k0 < total; k0 += 32) {  // warp-uniform trip count
+        const int k = k0 + lane;
+        int o = 0;  // owner lane: the first lane whose inclusive prefix exceeds k
+#pragma unroll
+        for (int st2 = 16; st2 > 0; st2 >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, incl, o + st2 - 1);
+          if (v <= k) o += st2;
+        }
+        const int ex_o = __shfl_sync(0xffffffffu, incl - rest, o);
+        const int c1_o = __shfl_sync(0xffffffffu, lc1, o);
+        const int own_o = __shfl_sync(0xffffffffu, own, o);
+        const unsigned long long mk_o = __shfl_sync(0xffffffffu, mk, o);
+        if (k < total) {
+          unsigned* col = (unsigned*)(own_o ? cb : ca);
+          const int c = c1_o + 4 + (k - ex_o);
+          if ((unsigned)mk_o) atomicOr(&col[2 * c], (unsigned)mk_o);
+          if ((unsigned)(mk_o >> 32)) atomicOr(&col[2 * c + 1], (unsigned)(mk_o >> 32));
+        }
+      }
+    }
+    if (tctr) { const long long qb = clock64(); qpaint += qb - qa; qa = qb; }
   }
   __syncwarp();
+  if (tctr && lane == 0) {
+    atomicAdd((unsigned long long*)&tctr[8], (unsigned long long)qsetup);
+    atomicAdd((unsigned long long*)&tctr[9], (unsigned long long)qpaint);
+  }
   for (int c = c0; c < c1e; ++c) ca[c] = gb_pred(op, ca[c], cb[c]);
   __syncwarp();
+  TSTEP(1)
   // ---- run starts S_c = R_c & ~R_{c-1}, transposed to one column bitmap per row
   const bool tr = L <= TK_LCN;
   if (tr) {
@@ -262,7 +301,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     }
     __syncwarp();
   }
-  TSTEP(1)
+  TSTEP(5)
 
   // ---- forward segmented OR-scan over the columns (bit-parallel over rows)
   auto R = [&](int c) -> unsigned long long { return (c < 0 || c >= L) ? 0ull : ca[c]; };
@@ -292,7 +331,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   TSTEP(2)
 
   // ---- count pieces / opens / heads
-  int np = 0, no = 0, nh = 0;
+  int np = 0, no = 0, nh = 0, ncn = 0;
   {
     unsigned long long Rm1 = R(c0 - 1), F = Fin;
     for (int c = c0; c < c1e; ++c) {
@@ -308,20 +347,22 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       if (!last_sb && (Ec >> 63)) ++no;
       const int cont = (sb > 0) && ((Z >> 1) & 1ull) && !((Chg >> 1) & 1ull);
       nh += pc - cont;
+      ncn += cont;
       Rm1 = Rc;
     }
   }
-  int totP, totO, totH;
+  int totP, totO, totH, totC;
   const int posP = gb_warp_excl(np, &totP);
   const int posO = gb_warp_excl(no, &totO);
   const int posH = gb_warp_excl(nh, &totH);
+  const int posC = gb_warp_excl(ncn, &totC);
   int pbase = 0;
   unsigned long long obase = 0;
   if (lane == 0) {
     pbase = (int)atomicAdd(&s.down, (unsigned long long)totP);
-    if (32ull * (unsigned long long)(pbase + totP) > scr - half) { s.err = 1; pbase = -1; }
-    if (totO > 0 && pbase >= 0) {
-      void* p = sc_up(s, base, half, (unsigned long long)totO * 4);
+    if (16ull * (unsigned long long)(pbase + totP) > scr - half) { s.err = 1; pbase = -1; }
+    if (totO + totC > 0 && pbase >= 0) {
+      void* p = sc_up(s, base, half, (unsigned long long)(totO + totC) * 4);
       obase = p ? (unsigned long long)((char*)p - base) : 0;
       if (!p) pbase = -1;
     }
@@ -329,13 +370,13 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   pbase = __shfl_sync(0xffffffffu, pbase, 0);
   obase = __shfl_sync(0xffffffffu, obase, 0);
   if (pbase < 0) return;
-  int* olist = (int*)(base + obase);
+  int* olist = (int*)(base + obase);  // open pieces, then continuation pieces, each in y order
   TSTEP(3)
 
   // ---- write pieces
   {
     unsigned long long Rm1 = R(c0 - 1), F = Fin;
-    int p = pbase + posP, o = posO, h = posH;
+    int p = pbase + posP, o = posO, h = posH, q = posC;
     for (int c = c0; c < c1e; ++c) {
       const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
       const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
@@ -366,17 +407,15 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         const int cont = (sb > 0) && (r == 1) && !((Chg >> 1) & 1ull);
         const int open = (rend == 64) && !last_sb;
         PieceRec pr;
-        pr.ylo = lv[cs];
-        pr.yhi = lv[c + 1];
-        pr.slo = rowbase + r;
-        pr.shi = (rowbase + rend) | (cont << 30) | (open << 31);
-        pr.hrank = cont ? -1 : h;
-        pr.sb = sb;
-        pr.pad0 = 0;
-        pr.pad1 = 0;
+        const unsigned hr = cont ? 0u : (unsigned)h;
+        pr.x = lv[cs] | (cont << 30) | (open << 31);
+        pr.y = lv[c + 1] | (int)((hr & 0x7fffu) << 17);
+        pr.z = (rowbase + r) | (int)((hr >> 15) << 17);
+        pr.w = rowbase + rend;
         if (!cont) ++h;
         *rec_at(base, scr, p) = pr;
         if (open) olist[o++] = p;
+        if (cont) olist[totO + q++] = p;
         ++p;
       }
       Rm1 = Rc;
@@ -386,6 +425,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   if (lane == 0) {
     s.sbinfo[sb] = make_int4(pbase, totP, (int)obase, totO);
     s.sbh[sb] = totH;
+    s.sbct[sb] = totC;
   }
 #undef TSTEP
 }
@@ -520,9 +560,10 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     if (tid == 0) {
       const int nwy = ((Ny - 1) >> 5) + 1;
-      s.mem = (int*)sc_up(s, base, half, (unsigned long long)M * 4);
+      s.mem = (int4*)sc_up(s, base, half, (unsigned long long)M * 16);
       s.sbinfo = (int4*)sc_up(s, base, half, (unsigned long long)nsb * 16);
       s.sbh = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
+      s.sbct = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
       s.biglb = nwy > TK_LBW ? (unsigned*)sc_up(s, base, half, (unsigned long long)TK_NW * 2 * nwy * 4)
                              : nullptr;
     }
@@ -531,7 +572,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       for (int i = tid; i < P; i += TK_NT) {
         const int4 r = s.rk[i];
         const int lo = r.x / 63, hi = min(nsb - 1, r.y / 63);
-        for (int q = lo; q <= hi; ++q) s.mem[atomicAdd(&s.sbc[q], 1)] = i;
+        const int4 rec = make_int4(r.x | (i >= nA ? (int)0x80000000 : 0), r.y, r.z, r.w);
+        for (int q = lo; q <= hi; ++q) s.mem[atomicAdd(&s.sbc[q], 1)] = rec;
       }
     }
     __syncthreads();
@@ -550,9 +592,14 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     __syncthreads();
     if (timing) { const long long t1 = clock64(); tC += t1 - t0; t0 = t1; }
-    // ---- D: stitch and emit
+    // ---- D: stitch and emit.  Piece records, chain links and the x / y value
+    // tables are staged in shared memory that phases A-C no longer use.
     const int NP = (int)s.down;
-    if (tid == 0 && !s.err) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
+    constexpr int DBYTES = (int)(sizeof(s.lb) + sizeof(s.lp) + sizeof(s.lv) + sizeof(s.ca) + sizeof(s.cb) +
+                                 sizeof(s.mc) + sizeof(s.srow));
+    const bool prs = (long long)NP * 20 <= DBYTES;
+    const bool xys = Nx + Ny <= 4 * TK_WMAX;
+    if (tid == 0 && !s.err && !prs) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
     __syncthreads();
     if (s.err) {
       if (tid == 0) {
@@ -562,7 +609,17 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       continue;
     }
-    for (int p = tid; p < NP; p += TK_NT) s.succ[p] = -1;
+    PieceRec* PR = prs ? reinterpret_cast<PieceRec*>(s.dbuf) : nullptr;
+    int* succ = prs ? reinterpret_cast<int*>(s.dbuf + (size_t)NP * 16) : s.succ;
+    const int* Xv = xys ? s.xyv : s.Xt;
+    const int* Yv = xys ? s.xyv + Nx : s.Yt;
+    if (prs)
+      for (int p = tid; p < NP; p += TK_NT) PR[p] = *rec_at(base, scr, p);
+    if (xys) {
+      for (int i = tid; i < Nx; i += TK_NT) s.xyv[i] = s.Xt[i];
+      for (int i = tid; i < Ny; i += TK_NT) s.xyv[Nx + i] = s.Yt[i];
+    }
+    for (int p = tid; p < NP; p += TK_NT) succ[p] = -1;
     int H = 0;
     {
       long long carry = 0;
@@ -577,22 +634,27 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       H = (int)carry;
     }
     __syncthreads();
+    // link every continuation piece to the open piece of the previous
+    // sub-band with the same y-interval (open lists are in y order)
     for (int p = tid; p < NP; p += TK_NT) {
-      const PieceRec pr = *rec_at(base, scr, p);
-      if (!((pr.shi >> 30) & 1)) continue;
-      const int4 inf = s.sbinfo[pr.sb - 1];
+      const PieceRec pr = prs ? PR[p] : *rec_at(base, scr, p);
+      if (!pr_cont(pr)) continue;
+      const int sbp = pr_slo(pr) / 63 - 1;
+      const int4 inf = s.sbinfo[sbp];
       const int* ol = (const int*)(base + inf.z);
+      const int y = pr_ylo(pr);
       int lo = 0, hi = inf.w - 1, q = -1;
       while (lo <= hi) {
         const int mid = (lo + hi) >> 1;
         const int cand = ol[mid];
-        const int y = rec_at(base, scr, cand)->ylo;
-        if (y == pr.ylo) { q = cand; break; }
-        if (y < pr.ylo) lo = mid + 1; else hi = mid - 1;
+        const int yc = pr_ylo(prs ? PR[cand] : *rec_at(base, scr, cand));
+        if (yc == y) { q = cand; break; }
+        if (yc < y) lo = mid + 1; else hi = mid - 1;
       }
-      if (q >= 0) s.succ[q] = p;
+      if (q >= 0) succ[q] = p;
       else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
     }
+    __syncthreads();
     if (tid == 0) {
       s.obase = -1;
       if (mode == 0 && H > 0) {
@@ -612,13 +674,14 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     unsigned long long* outp = obase >= 0 ? O->pcs + obase : nullptr;
     long long area = 0;
     for (int p = tid; p < NP; p += TK_NT) {
-      const PieceRec pr = *rec_at(base, scr, p);
-      if ((pr.shi >> 30) & 1) continue;
+      const PieceRec pr = prs ? PR[p] : *rec_at(base, scr, p);
+      if (pr_cont(pr)) continue;
       int q = p, guard = 0;
-      while (s.succ[q] >= 0 && guard++ <= nsb) q = s.succ[q];
-      const int shi = rec_at(base, scr, q)->shi & 0x3fffffff;
-      const int xs = s.Xt[pr.slo], xe = s.Xt[shi], ylo = s.Yt[pr.ylo], yhi = s.Yt[pr.yhi];
-      const int pos = s.sbh[pr.sb] + pr.hrank;
+      while (succ[q] >= 0 && guard++ <= nsb) q = succ[q];
+      const int shi = q == p ? pr_shi(pr) : pr_shi(prs ? PR[q] : *rec_at(base, scr, q));
+      const int slo = pr_slo(pr);
+      const int xs = Xv[slo], xe = Xv[shi], ylo = Yv[pr_ylo(pr)], yhi = Yv[pr_yhi(pr)];
+      const int pos = s.sbh[slo / 63] + pr_hrank(pr);
       if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
       area += (long long)(xe - xs) * (long long)(yhi - ylo);
     }
