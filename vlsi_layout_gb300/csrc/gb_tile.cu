@@ -749,3 +749,187 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
   if (c.prof) cudaEventRecordWithFlags(e1, c.stream, c.prof_flags);
   c.launches += 2;
 }
+
+// ===================================================================== no-allocation entry point
+// gb_bool_tile_noalloc: the scanline Boolean for callers that cannot allocate
+// device memory -- code running where cudaMalloc is not permitted on the
+// request path (a serving loop that has reserved its whole device budget up
+// front, a host that must not take the allocator's implicit device-wide
+// synchronisation, or a Fortran/C caller that only owns the buffers it
+// passes).  It computes the canonical strips of pred(A, B) for boxes that all
+// lie inside one 65536-dbu tile, entirely in memory reserved statically in
+// this library: every GPU that loads libgbool.so holds this storage until the
+// process exits.
+//
+// Limits: nA + nB <= GB_NA_MAX_IN boxes, at most GB_NA_MAX_OUT result strips,
+// and the CTA scratch of GB_NA_SCRATCH bytes.  Beyond any of them the call
+// returns GB_ERR_CAPACITY and leaves *d_count at -1.
+//
+// All calls share the static storage (each call re-initialises what must
+// start at zero and keeps the last call's contents otherwise), so calls whose
+// work overlaps on the GPU -- on different streams, or from different host
+// threads -- race and must be serialised by the caller.
+//
+// Set-up: the first call on a device resolves the device addresses of the
+// static storage with cudaGetSymbolAddress (with that device current) and
+// sets the kernel's shared-memory attribute; later calls on that device reuse
+// them.  Make that first call before any stream capture.
+#define GB_NA_MAX_IN 16384
+#define GB_NA_MAX_OUT 65536
+#define GB_NA_SCRATCH (8u << 20)
+#define GB_NA_MAX_DEV 64
+
+struct NoAllocState {
+  DLayer L[3];                              // A, B, result
+  DStatus st;                               // status; its arena is empty (no spill space)
+  long long ctr[64];                        // work counters of the tile kernel
+  int4 win[3];
+  long long tbase[3][2];
+  long long tstart[3][2];
+  int tcount[3][2];
+  long long cell_count[3];
+  long long cell_area[3];
+  int4 cbox[3];
+  unsigned long long pcs_in[GB_NA_MAX_IN];  // packed pieces of A then B
+  unsigned long long pcs_out[GB_NA_MAX_OUT];
+};
+
+static __device__ __align__(256) NoAllocState g_na_state;
+static __device__ __align__(256) char g_na_scratch[GB_NA_SCRATCH];
+
+static NoAllocState* g_na_state_ptr[GB_NA_MAX_DEV];
+static char* g_na_scratch_ptr[GB_NA_MAX_DEV];
+static std::mutex g_na_mu;
+
+// Re-initialise the shared state and pack the inputs (one block).  Every box
+// must lie inside the tile of the first box; otherwise the status says so.
+__global__ void k_na_prep(NoAllocState* S, int op, const int4* A, int nA, const int4* B, int nB, int g) {
+  __shared__ int bad;
+  __shared__ int tx0, ty0;
+  if (threadIdx.x == 0) {
+    bad = 0;
+    const int4 f = nA ? A[0] : (nB ? B[0] : make_int4(0, 0, 1, 1));
+    tx0 = gb_floor_shift(f.x, g);
+    ty0 = gb_floor_shift(f.y, g);
+    memset(&S->st, 0, sizeof(S->st));  // empty arena: spills report GB_ERR_CAPACITY
+    for (int i = 0; i < 64; ++i) S->ctr[i] = 0;
+  }
+  __syncthreads();
+  const int n = nA + nB;
+  const int ox = tx0 << g, oy = ty0 << g;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int4 b = i < nA ? A[i] : B[i - nA];
+    const bool ok = b.x < b.z && b.y < b.w && gb_floor_shift(b.x, g) == tx0 &&
+                    gb_floor_shift(b.z - 1, g) == tx0 && gb_floor_shift(b.y, g) == ty0 &&
+                    gb_floor_shift(b.w - 1, g) == ty0;
+    if (!ok) { atomicOr(&bad, 1); continue; }
+    S->pcs_in[i] = gb_pack(b.x - ox, b.y - oy, b.z - ox, b.w - oy);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bad) gb_set_error(&S->st, GB_ERR_INVALID_BOX, 60, 0);
+    for (int l = 0; l < 3; ++l) {
+      DLayer& d = S->L[l];
+      memset(&d, 0, sizeof(d));
+      d.ncell = 1;
+      d.g = g;
+      d.binned = 1;
+      S->win[l] = make_int4(tx0, ty0, 1, 1);
+      S->tbase[l][0] = 0;
+      S->tbase[l][1] = 1;
+      S->cell_count[l] = 0;
+      S->cell_area[l] = 0;
+      S->cbox[l] = make_int4(ox, oy, ox + (1 << g), oy + (1 << g));
+      d.win = &S->win[l];
+      d.tbase = S->tbase[l];
+      d.tstart = S->tstart[l];
+      d.tcount = S->tcount[l];
+      d.cell_count = &S->cell_count[l];
+      d.cell_area = &S->cell_area[l];
+      d.cbox = &S->cbox[l];
+      d.ntiles = 1;
+    }
+    S->L[0].pcs = S->pcs_in;
+    S->tstart[0][0] = 0;
+    S->tcount[0][0] = nA;
+    S->L[0].npcs = S->L[0].nused = S->L[0].ntot = nA;
+    S->L[1].pcs = S->pcs_in;
+    S->tstart[1][0] = nA;
+    S->tcount[1][0] = op == GB_OP_MERGE ? 0 : nB;
+    S->L[1].npcs = S->L[1].nused = S->L[1].ntot = nB;
+    S->L[2].pcs = S->pcs_out;
+    S->L[2].npcs = GB_NA_MAX_OUT;
+    S->tstart[2][0] = 0;
+    S->tcount[2][0] = 0;
+    if (bad) S->L[2].ntiles = 0;  // nothing runs on invalid input
+  }
+}
+
+// Unpack the result into the caller's buffer; *count = strips, or -1 when the
+// call failed or the buffer is too small.
+__global__ void k_na_export(const NoAllocState* S, int4* out, long long cap, long long* count, long long* area) {
+  const DLayer& O = S->L[2];
+  const long long n = O.ntiles ? O.tcount[0] : 0;
+  const bool ok = S->st.err == 0 && n <= cap;
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    *count = ok ? n : -1;
+    if (area) *area = ok ? S->cell_area[2] : -1;
+  }
+  if (!ok) return;
+  const int4 w = S->win[2];
+  const int ox = w.x << O.g, oy = w.y << O.g;
+  const unsigned long long* p = O.pcs + O.tstart[0];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int a, b, c, d;
+    gb_unpack(p[i], a, b, c, d);
+    out[i] = make_int4(ox + a, oy + b, ox + c, oy + d);
+  }
+}
+
+extern "C" int gb_bool_tile_noalloc(int op, const int4* d_A, int nA, const int4* d_B, int nB, int4* d_out,
+                                    long long out_cap, long long* d_count, long long* d_area, void* stream) {
+  if (op < GB_OP_XOR || op > GB_OP_MERGE || nA < 0 || nB < 0 || !d_out || !d_count) return GB_ERR_ARG;
+  if ((long long)nA + nB > GB_NA_MAX_IN) {
+    fprintf(stderr, "gb_bool_tile_noalloc: %lld input boxes exceed the static limit of %d\n",
+            (long long)nA + nB, GB_NA_MAX_IN);
+    return GB_ERR_CAPACITY;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= GB_NA_MAX_DEV) return GB_ERR_CUDA;
+  NoAllocState* S;
+  char* scr;
+  {
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_state_ptr[dev]) {
+      void* a = nullptr;
+      void* b = nullptr;
+      if (cudaGetSymbolAddress(&a, g_na_state) != cudaSuccess ||
+          cudaGetSymbolAddress(&b, g_na_scratch) != cudaSuccess) {
+        fprintf(stderr, "gb_bool_tile_noalloc: cudaGetSymbolAddress failed on device %d\n", dev);
+        return GB_ERR_CUDA;
+      }
+      if (cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)) !=
+          cudaSuccess)
+        return GB_ERR_CUDA;
+      g_na_state_ptr[dev] = (NoAllocState*)a;
+      g_na_scratch_ptr[dev] = (char*)b;
+    }
+    S = g_na_state_ptr[dev];
+    scr = g_na_scratch_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int g = 16;
+  k_na_prep<<<1, 256, 0, s>>>(S, op, d_A, nA, d_B, nB, g);
+  k_tile<<<1, TK_NT, sizeof(TileSmem), s>>>(op, &S->L[0], &S->L[1], &S->L[2], g, 0, scr, GB_NA_SCRATCH, S->ctr,
+                                            &S->st);
+  k_na_export<<<8, 256, 0, s>>>(S, d_out, out_cap, d_count, d_area);
+  if (cudaGetLastError() != cudaSuccess) return GB_ERR_CUDA;
+  DStatus hs;
+  if (cudaMemcpyAsync(&hs, &S->st, sizeof(hs), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return GB_ERR_CUDA;
+  if (hs.err == GB_ERR_CAPACITY)
+    fprintf(stderr, "gb_bool_tile_noalloc: result exceeds the static limits (%d strips, %u scratch bytes)\n",
+            GB_NA_MAX_OUT, GB_NA_SCRATCH);
+  return hs.err;
+}

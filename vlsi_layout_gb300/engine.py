@@ -89,6 +89,7 @@ def lib():
         "gb_profile": (ctypes.c_int, [P, ctypes.c_int]),
         "gb_profile_read": (ctypes.c_int, [P, P, P, P, P]),
         "gb_launch_count": (i64, [P]),
+        "gb_bool_tile_noalloc": (ctypes.c_int, [ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, i64, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
