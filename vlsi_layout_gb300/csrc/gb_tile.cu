@@ -67,9 +67,10 @@ __device__ __forceinline__ int pr_hrank(const PieceRec& p) {
 struct TileSmem {
   union {  // phases A-B: value bitmaps and their prefix popcounts; phase D: x / y value tables
     struct {
-      unsigned xb[TK_WMAX], xp[TK_WMAX], yb[TK_WMAX], yp[TK_WMAX];
+      unsigned xb[TK_WMAX], yb[TK_WMAX];
+      unsigned xp[TK_WMAX / 4 + 1], yp[TK_WMAX / 4 + 1];  // prefix popcount per 4 words
     };
-    int xyv[4 * TK_WMAX];
+    int xyv[2 * TK_WMAX + 2 * (TK_WMAX / 4 + 1)];
   };
   int sbc[TK_NSBMAX + 2];
   union {  // phase C: per-warp sweep buffers; phase D: piece records and chain links
@@ -115,6 +116,13 @@ __device__ __forceinline__ unsigned long long gb_pred(int op, unsigned long long
 __device__ __forceinline__ int bm_rank(const unsigned* bits, const unsigned* pref, int v) {
   const int w = v >> 5;
   return (int)pref[w] + __popc(bits[w] & ((1u << (v & 31)) - 1u));
+}
+// rank with a prefix stored once per 4 words
+__device__ __forceinline__ int bm_rank4(const unsigned* bits, const unsigned* pref4, int v) {
+  const int w = v >> 5, w0 = w & ~3;
+  int r = (int)pref4[w >> 2];
+  for (int k = w0; k < w; ++k) r += __popc(bits[k]);
+  return r + __popc(bits[w] & ((1u << (v & 31)) - 1u));
 }
 
 __device__ __forceinline__ unsigned long long vchg(unsigned long long r) { return (r ^ (r << 1)) & ~1ull; }
@@ -430,7 +438,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
 #undef TSTEP
 }
 
-__global__ void __launch_bounds__(TK_NT, 2)
+__global__ void __launch_bounds__(TK_NT, 3)
 k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, char* scratch,
        unsigned long long scr, long long* counter, DStatus* st) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -497,15 +505,16 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     __syncthreads();
     int Nx, Ny;
     {
-      const int per = (W + TK_NT - 1) / TK_NT, w0 = min(W, tid * per), w1 = min(W, w0 + per);
+      const int per = ((W + TK_NT - 1) / TK_NT + 3) & ~3, w0 = min(W, tid * per), w1 = min(W, w0 + per);
       long long cx = 0, cy = 0;
       for (int w = w0; w < w1; ++w) { cx += __popc(s.xb[w]); cy += __popc(s.yb[w]); }
       long long tot;
       const long long ex = gb_block_excl(cx | (cy << 32), s.tmp64, &tot);
       unsigned ox = (unsigned)(ex & 0xffffffffll), oy = (unsigned)(ex >> 32);
       for (int w = w0; w < w1; ++w) {
-        s.xp[w] = ox; ox += __popc(s.xb[w]);
-        s.yp[w] = oy; oy += __popc(s.yb[w]);
+        if ((w & 3) == 0) { s.xp[w >> 2] = ox; s.yp[w >> 2] = oy; }
+        ox += __popc(s.xb[w]);
+        oy += __popc(s.yb[w]);
       }
       Nx = (int)(tot & 0xffffffffll);
       Ny = (int)(tot >> 32);
@@ -516,13 +525,12 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       __syncthreads();
       if (!s.err) {
+        int kx = w0 < W ? (int)s.xp[w0 >> 2] : 0, ky = w0 < W ? (int)s.yp[w0 >> 2] : 0;
         for (int w = w0; w < w1; ++w) {
           unsigned bits = s.xb[w];
-          int k = s.xp[w];
-          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Xt[k++] = (w << 5) + b; }
+          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Xt[kx++] = (w << 5) + b; }
           bits = s.yb[w];
-          k = s.yp[w];
-          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Yt[k++] = (w << 5) + b; }
+          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Yt[ky++] = (w << 5) + b; }
         }
       }
     }
@@ -537,8 +545,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
         int x1, y1, x2, y2;
         gb_unpack(pk, x1, y1, x2, y2);
-        const int r1 = bm_rank(s.xb, s.xp, x1), r2 = bm_rank(s.xb, s.xp, x2);
-        const int c1 = bm_rank(s.yb, s.yp, y1), c2 = bm_rank(s.yb, s.yp, y2);
+        const int r1 = bm_rank4(s.xb, s.xp, x1), r2 = bm_rank4(s.xb, s.xp, x2);
+        const int c1 = bm_rank4(s.yb, s.yp, y1), c2 = bm_rank4(s.yb, s.yp, y2);
         s.rk[i] = make_int4(r1, r2, c1, c2);
         const int lo = r1 / 63, hi = min(nsb - 1, r2 / 63);
         for (int q = lo; q <= hi; ++q) atomicAdd(&s.sbc[q], 1);
@@ -598,7 +606,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     constexpr int DBYTES = (int)(sizeof(s.lb) + sizeof(s.lp) + sizeof(s.lv) + sizeof(s.ca) + sizeof(s.cb) +
                                  sizeof(s.mc) + sizeof(s.srow));
     const bool prs = (long long)NP * 20 <= DBYTES;
-    const bool xys = Nx + Ny <= 4 * TK_WMAX;
+    const bool xys = Nx + Ny <= 2 * TK_WMAX + 2 * (TK_WMAX / 4 + 1);
     if (tid == 0 && !s.err && !prs) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
     __syncthreads();
     if (s.err) {
