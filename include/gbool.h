@@ -190,6 +190,13 @@ int32_t gb_um_to_dbu(double r);
 int gb_bool_tile_noalloc(int op, const c_box* d_A, int nA, const c_box* d_B, int nB, c_box* d_out,
                          long long out_cap, long long* d_count, long long* d_area, void* stream);
 
+/* ---- control decks */
+/* Run a MAGPARSER control deck (controlparser.f90 syntax; the README's
+ * RUN_LOOP(`OP1', ...) macro line is expanded in place) on the GPU engine.
+ * log (may be NULL) receives the interpreter's report; *assert_failures
+ * counts failed ASSERT_ZEROs.  Returns GB_OK or the first failing status. */
+int gb_run_deck(const char* path, char* log, unsigned long long log_cap, int* assert_failures);
+
 /* ---- deck-level execution */
 /* OP1 ring-check chain (op_template.m4:14-22) on all cells of P with amount a
  * dbu: outs[0..5] = P_1 (GROW a), P_2 (SIZE -a), outer ring (P_1 ~ P),

@@ -89,6 +89,7 @@ def lib():
         "gb_profile": (ctypes.c_int, [P, ctypes.c_int]),
         "gb_profile_read": (ctypes.c_int, [P, P, P, P, P]),
         "gb_launch_count": (i64, [P]),
+        "gb_run_deck": (ctypes.c_int, [ctypes.c_char_p, P, u64, P]),
         "gb_bool_tile_noalloc": (ctypes.c_int, [ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, i64, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -310,6 +311,14 @@ def event_sort(trackers):
     t = np.ascontiguousarray(trackers, dtype=TRACKER_DTYPE).copy()
     lib().device_event_sort(t.ctypes.data, len(t))
     return t
+
+
+def run_deck(path, log_cap=1 << 20):
+    """Run a control deck on the GPU engine; returns (status, log, assert_failures)."""
+    buf = ctypes.create_string_buffer(log_cap)
+    fails = ctypes.c_int()
+    rc = lib().gb_run_deck(os.fsencode(path), buf, log_cap, ctypes.byref(fails))
+    return rc, buf.value.decode(errors="replace"), fails.value
 
 
 def um_to_dbu(r):
