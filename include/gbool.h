@@ -197,6 +197,37 @@ int gb_bool_tile_noalloc(int op, const c_box* d_A, int nA, const c_box* d_B, int
  * counts failed ASSERT_ZEROs.  Returns GB_OK or the first failing status. */
 int gb_run_deck(const char* path, char* log, unsigned long long log_cap, int* assert_failures);
 
+/* ---- serving loop: Boolean requests on layers resident in HBM */
+#define GB_REQ_SIZE 5 /* request op: SIZE by `amount` dbu (ops 0..3 are the Booleans) */
+#define GB_REQ_GROW 6 /* request op: GROW all four sides by `amount` dbu */
+typedef struct gb_server gb_server;
+typedef struct gb_request {
+  int op;           /* GB_OP_XOR/OR/AND/NOT, GB_REQ_SIZE or GB_REQ_GROW */
+  int a, b;         /* resident layer ids (b unused by SIZE / GROW) */
+  int amount;       /* dbu for SIZE / GROW */
+  double arrival_s; /* arrival time, seconds after the start of gb_serve_run */
+} gb_request;
+typedef struct gb_result {
+  int status;       /* GB_* of the request */
+  int pad;
+  long long count;  /* strips in the result */
+  double start_s, end_s, latency_ms; /* admission, completion, completion - arrival */
+} gb_result;
+/* A server with `slots` concurrent execution slots (each its own stream and
+ * work arena of slot_arena_bytes) admitting requests while the estimated
+ * device memory of those in flight stays within budget_bytes. */
+int gb_serve_create(int device, unsigned long long budget_bytes, int slots,
+                    unsigned long long slot_arena_bytes, gb_server** out);
+/* Add a resident layer (copied to HBM and binned once). */
+int gb_serve_add_layer(gb_server* s, const c_box* boxes, unsigned long long n, int* id);
+/* Serve requests in arrival order on the host clock (requests sorted by
+ * arrival_s); a request is admitted when it has arrived, a slot is free and
+ * the memory budget allows; results[i] gets its status, strip count and
+ * latency.  keep_outputs != 0 keeps every result for gb_serve_result_boxes. */
+int gb_serve_run(gb_server* s, const gb_request* reqs, int nreq, gb_result* results, int keep_outputs);
+int gb_serve_result_boxes(gb_server* s, int index, c_box* out, unsigned long long cap, unsigned long long* n);
+void gb_serve_destroy(gb_server* s);
+
 /* ---- deck-level execution */
 /* OP1 ring-check chain (op_template.m4:14-22) on all cells of P with amount a
  * dbu: outs[0..5] = P_1 (GROW a), P_2 (SIZE -a), outer ring (P_1 ~ P),

@@ -90,6 +90,11 @@ def lib():
         "gb_profile_read": (ctypes.c_int, [P, P, P, P, P]),
         "gb_launch_count": (i64, [P]),
         "gb_run_deck": (ctypes.c_int, [ctypes.c_char_p, P, u64, P]),
+        "gb_serve_create": (ctypes.c_int, [ctypes.c_int, u64, ctypes.c_int, u64, pp]),
+        "gb_serve_add_layer": (ctypes.c_int, [P, P, u64, P]),
+        "gb_serve_run": (ctypes.c_int, [P, P, ctypes.c_int, P, ctypes.c_int]),
+        "gb_serve_result_boxes": (ctypes.c_int, [P, ctypes.c_int, P, u64, P]),
+        "gb_serve_destroy": (None, [P]),
         "gb_bool_tile_noalloc": (ctypes.c_int, [ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, i64, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -311,6 +316,59 @@ def event_sort(trackers):
     t = np.ascontiguousarray(trackers, dtype=TRACKER_DTYPE).copy()
     lib().device_event_sort(t.ctypes.data, len(t))
     return t
+
+
+REQ_SIZE, REQ_GROW = 5, 6
+REQUEST_DTYPE = np.dtype([("op", np.int32), ("a", np.int32), ("b", np.int32), ("amount", np.int32),
+                          ("arrival_s", np.float64)])
+RESULT_DTYPE = np.dtype([("status", np.int32), ("pad", np.int32), ("count", np.int64), ("start_s", np.float64),
+                         ("end_s", np.float64), ("latency_ms", np.float64)])
+
+
+class Server:
+    """Request loop over layers resident in HBM (gb_serve_*): continuous
+    admission into concurrent slots under a device-memory budget."""
+
+    def __init__(self, device=0, budget_bytes=120 << 30, slots=8, slot_arena_bytes=8 << 30):
+        h = ctypes.c_void_p()
+        rc = lib().gb_serve_create(device, budget_bytes, slots, slot_arena_bytes, ctypes.byref(h))
+        if rc != GB_OK:
+            raise GBError(rc, "gb_serve_create failed")
+        self.h = h
+
+    def add_layer(self, boxes):
+        b = _boxes(boxes)
+        i = ctypes.c_int()
+        rc = lib().gb_serve_add_layer(self.h, b.ctypes.data, len(b), ctypes.byref(i))
+        if rc != GB_OK:
+            raise GBError(rc, "gb_serve_add_layer failed")
+        return i.value
+
+    def run(self, requests, keep_outputs=False):
+        r = np.ascontiguousarray(requests, REQUEST_DTYPE)
+        out = np.zeros(len(r), RESULT_DTYPE)
+        rc = lib().gb_serve_run(self.h, r.ctypes.data, len(r), out.ctypes.data, 1 if keep_outputs else 0)
+        if rc != GB_OK:
+            raise GBError(rc, "gb_serve_run failed")
+        return out
+
+    def result_boxes(self, i):
+        n = ctypes.c_uint64()
+        lib().gb_serve_result_boxes(self.h, i, None, 0, ctypes.byref(n))
+        out = np.zeros((max(1, n.value), 4), np.int32)
+        lib().gb_serve_result_boxes(self.h, i, out.ctypes.data, n.value, ctypes.byref(n))
+        return out[:n.value]
+
+    def close(self):
+        if self.h:
+            lib().gb_serve_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def run_deck(path, log_cap=1 << 20):
