@@ -143,6 +143,41 @@ def cpu_leg(boxes, off, seconds=15.0):
             "sample": "OP1 + union area on the first %d cells (%d boxes), %.1f s" % (k, int(off[k]), dt)}
 
 
+def serve_leg(rates=(1000, 10000), seconds=0.5, max_req=3000, seed=4, slots=8):
+    """cfg4-style serving: 64 resident layers (cfg0-style, lognormal sizes in
+    [1k, 20M], median 30k), Poisson arrivals, op uniform over AND / NOT / OR /
+    XOR / GROW / SIZE, operands uniform; 120 GB admission budget."""
+    from vlsi_layout_gb300 import engine
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.round(rng.lognormal(np.log(30000), 1.5, 64)), 1000, 20_000_000).astype(np.int64)
+    out = {"layers": 64, "resident_boxes": int(sizes.sum()), "budget_gb": 120, "slots": slots, "rates": []}
+    with engine.Server(budget_bytes=120 << 30, slots=slots, slot_arena_bytes=8 << 30) as S:
+        for k, n in enumerate(sizes):
+            b, _ = make_cells(1, median=int(n), sigma=1e-9, lo=int(n), hi=int(n), seed=seed * 1000 + k)
+            S.add_layer(b)
+        ops = np.array([2, 3, 1, 0, engine.REQ_GROW, engine.REQ_SIZE])
+        for lam in rates:
+            n = int(min(max_req, lam * seconds))
+            r = np.zeros(n, engine.REQUEST_DTYPE)
+            r["op"] = ops[rng.integers(0, 6, n)]
+            r["a"] = rng.integers(0, 64, n)
+            r["b"] = rng.integers(0, 64, n)
+            r["amount"] = np.where(r["op"] == engine.REQ_SIZE, np.where(rng.random(n) < 0.5, -1, 1), 1)
+            r["arrival_s"] = np.cumsum(rng.exponential(1.0 / lam, n))
+            t0 = time.perf_counter()
+            res = S.run(r)
+            wall = time.perf_counter() - t0
+            ok = res["status"] == 0
+            boxes = sizes[r["a"]] + np.where(r["op"] <= 3, sizes[r["b"]], 0)
+            lat = res["latency_ms"][ok]
+            out["rates"].append({"lambda_req_s": lam, "requests": n, "ok": int(ok.sum()),
+                                 "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                                 "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                                 "served_req_s": float(ok.sum() / wall),
+                                 "boxes_per_s": float(boxes[ok].sum() / wall)})
+    return out
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -202,8 +237,17 @@ def main():
     ap.add_argument("--ref-boxes", type=int, default=600_000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true")
+    ap.add_argument("--serve-rates", default="1000,10000")
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
+    if args.serve_only:
+        import torch
+        torch.cuda.set_device(local)
+        rates = tuple(int(x) for x in args.serve_rates.split(","))
+        print(json.dumps({"serving": serve_leg(rates=rates, seconds=2.0, max_req=20000)}), flush=True)
+        return
     boxes, off = make_cells(args.cells, args.median, seed=args.seed)
     nbox = int(off[-1])
     if args.impl == "reference":
@@ -329,6 +373,10 @@ def main():
     if rank == 0 and not args.no_cpu:
         cpu = cpu_leg(boxes, off, args.cpu_seconds)
 
+    ctx.close()
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = serve_leg(rates=tuple(int(x) for x in args.serve_rates.split(",")))
     value = world * nbox / (ms / 1e3)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
@@ -355,10 +403,10 @@ def main():
         "clocks": clocks,
         "assert_zero_failures": fails,
         "parity": parity,
+        "serving": serving,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
-    ctx.close()
     if dist:
         dist.destroy_process_group()
 
