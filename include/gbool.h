@@ -266,6 +266,10 @@ long long gb_launch_count(gb_context* ctx);
  * pieces; then per-warp cycles of the sub-band steps (compress, rasterise,
  * scan, count, write), members and columns, since gb_tile_timing(ctx, 1). */
 int gb_tile_timing(gb_context* ctx, int on);
+/* Diagnostics: runs one radix pass whose only CTA waits for a predecessor
+ * tile that never publishes; returns the status it reports (GB_ERR_TIMEOUT
+ * when the bounded wait works) with the context status cleared again. */
+int gb_debug_lookback_timeout(gb_context* ctx, int spin_limit);
 int gb_tile_timing_read(gb_context* ctx, long long* out8);
 
 #ifdef __cplusplus

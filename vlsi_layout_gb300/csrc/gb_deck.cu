@@ -215,3 +215,12 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
   gb_layer_free(ctx, P);
   return e;
 }
+
+extern "C" int gb_debug_lookback_timeout(gb_context* ctx, int spin_limit) {
+  if (!ctx || spin_limit < 1) return GB_ERR_ARG;
+  gb_clear_status(ctx);
+  if (gb_radix_lookback_timeout_probe(ctx->c, spin_limit)) return GB_ERR_CUDA;
+  const int e = gb_sync(ctx, nullptr);
+  gb_clear_status(ctx);
+  return e;
+}

@@ -126,6 +126,8 @@ void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* pare
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
                         unsigned long long* keys_tmp, unsigned* vals_tmp, int digit_bits);
 
+int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit);
+
 // helpers
 inline int gb_cuda_check(GbCtx& c, cudaError_t e, const char* what) {
   if (e != cudaSuccess) {

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict__ vin,
           unsigned long long* __restrict__ kout, unsigned* __restrict__ vout, long long n, int shift,
           int dbits, const unsigned* __restrict__ gofs, unsigned long long* status,
-          unsigned long long epoch, long long* counter, DStatus* st) {
+          unsigned long long epoch, long long* counter, DStatus* st, int spin_limit) {
   extern __shared__ __align__(16) unsigned char smraw[];
   RsSmem& s = *reinterpret_cast<RsSmem*>(smraw);
   const int lane = gb_lane(), wid = gb_warp();
@@ -136,7 +136,7 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
         const unsigned long long w = *(volatile unsigned long long*)(status + (size_t)j * RS_RADIX + d);
         const unsigned long long flag = (w >> 46) & 3ull;
         if ((w & 0xFFFF000000000000ull) != etag || flag == 0) {
-          if (++spins > RS_SPIN_LIMIT) {
+          if (++spins > spin_limit) {
             gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX, j);
             break;
           }
@@ -228,7 +228,7 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     }
     k_rs_pass<<<(unsigned)ntile, RS_THREADS, sizeof(RsSmem), c.stream>>>(
         ka, va, kb, vb, n, p * digit_bits, digit_bits, g_rs.ghist + p * RS_RADIX, g_rs.status,
-        g_rs.epoch, g_rs.ctrs + p, c.st);
+        g_rs.epoch, g_rs.ctrs + p, c.st, RS_SPIN_LIMIT);
     std::swap(ka, kb);
     std::swap(va, vb);
   }
@@ -237,4 +237,28 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     cudaMemcpyAsync(vals, va, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
   }
   return passes;
+}
+
+// Diagnostics for the bounded look-back: one CTA is handed tile 1 of a
+// two-tile pass, so it waits for a tile-0 status word that nothing ever
+// publishes.  After spin_limit polls it must flag GB_ERR_TIMEOUT and finish.
+__global__ void k_rs_set_counter(long long* c, long long v) { *c = v; }
+int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit) {
+  const long long n = 2 * RS_TILE;
+  unsigned long long *k = nullptr, *k2 = nullptr, *status = nullptr;
+  unsigned *v = nullptr, *v2 = nullptr, *gofs = nullptr;
+  long long* ctr = nullptr;
+  cudaMalloc(&k, n * 8); cudaMalloc(&k2, n * 8); cudaMalloc(&v, n * 4); cudaMalloc(&v2, n * 4);
+  cudaMalloc(&status, 2 * RS_RADIX * 8); cudaMalloc(&gofs, RS_RADIX * 4); cudaMalloc(&ctr, 8);
+  cudaMemsetAsync(k, 0, n * 8, c.stream);
+  cudaMemsetAsync(v, 0, n * 4, c.stream);
+  cudaMemsetAsync(status, 0, 2 * RS_RADIX * 8, c.stream);
+  cudaMemsetAsync(gofs, 0, RS_RADIX * 4, c.stream);
+  k_rs_set_counter<<<1, 1, 0, c.stream>>>(ctr, 1);
+  cudaFuncSetAttribute(k_rs_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem));
+  k_rs_pass<<<1, RS_THREADS, sizeof(RsSmem), c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st,
+                                                        spin_limit);
+  const cudaError_t e = cudaStreamSynchronize(c.stream);
+  cudaFree(k); cudaFree(k2); cudaFree(v); cudaFree(v2); cudaFree(status); cudaFree(gofs); cudaFree(ctr);
+  return e == cudaSuccess ? 0 : -1;
 }

@@ -90,6 +90,7 @@ def lib():
         "gb_profile_read": (ctypes.c_int, [P, P, P, P, P]),
         "gb_launch_count": (i64, [P]),
         "gb_run_deck": (ctypes.c_int, [ctypes.c_char_p, P, u64, P]),
+        "gb_debug_lookback_timeout": (ctypes.c_int, [P, ctypes.c_int]),
         "gb_serve_create": (ctypes.c_int, [ctypes.c_int, u64, ctypes.c_int, u64, pp]),
         "gb_serve_add_layer": (ctypes.c_int, [P, P, u64, P]),
         "gb_serve_run": (ctypes.c_int, [P, P, ctypes.c_int, P, ctypes.c_int]),
