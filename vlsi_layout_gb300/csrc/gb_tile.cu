@@ -92,6 +92,7 @@ struct TileSmem {
   const unsigned long long* pb;
   int nA, nB, cell, err;
   long long obase;
+  DStatus* st;
   unsigned long long up, down;  // scratch bump: bytes (low half) / 32-byte records (high half)
   int* Xt;
   int* Yt;
@@ -100,6 +101,8 @@ struct TileSmem {
   int4* sbinfo;  // per sub-band: piece base, piece count, open-list byte offset, open count
   int* sbh;      // heads per sub-band, then their exclusive scan
   int* sbct;     // continuation pieces per sub-band
+  int** sbol;    // open list (then continuation list) per sub-band
+  PieceRec** sbrec;  // strip pieces per sub-band (global piece index = sbinfo.x + local index)
   unsigned* biglb;
   int* succ;
 };
@@ -128,19 +131,19 @@ __device__ __forceinline__ int bm_rank4(const unsigned* bits, const unsigned* pr
 __device__ __forceinline__ unsigned long long vchg(unsigned long long r) { return (r ^ (r << 1)) & ~1ull; }
 
 // Allocation in the lower half of the CTA's scratch (one thread calls it).
+// When a dense tile outgrows it, the allocation spills into the work arena
+// (released with the operation); only an exhausted arena is an error.
 __device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long long half,
                                        unsigned long long bytes) {
   const unsigned long long off = atomicAdd(&s.up, (bytes + 15ull) & ~15ull);
   if (off + bytes > half) {
-    s.err = 1;
-    return nullptr;
+    void* p = s.st ? gb_arena_alloc_atomic(s.st, bytes, KID_TILE) : nullptr;
+    if (!p) s.err = 1;
+    return p;
   }
   return base + off;
 }
 
-__device__ __forceinline__ PieceRec* rec_at(char* base, unsigned long long scr, int p) {
-  return reinterpret_cast<PieceRec*>(base + scr - 16ull * (unsigned long long)(p + 1));
-}
 
 __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int nA, char* base,
                              unsigned long long scr, long long* tctr) {
@@ -151,7 +154,13 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
   const int m = end - beg;
   if (m == 0) {
-    if (lane == 0) { s.sbinfo[sb] = make_int4(0, 0, 0, 0); s.sbh[sb] = 0; s.sbct[sb] = 0; }
+    if (lane == 0) {
+      s.sbinfo[sb] = make_int4(0, 0, 0, 0);
+      s.sbh[sb] = 0;
+      s.sbct[sb] = 0;
+      s.sbol[sb] = nullptr;
+      s.sbrec[sb] = nullptr;
+    }
     return;
   }
   const int rowbase = 63 * sb - 1;
@@ -365,20 +374,26 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int posH = gb_warp_excl(nh, &totH);
   const int posC = gb_warp_excl(ncn, &totC);
   int pbase = 0;
-  unsigned long long obase = 0;
+  unsigned long long obase = 0, rbase = 0;
   if (lane == 0) {
     pbase = (int)atomicAdd(&s.down, (unsigned long long)totP);
-    if (16ull * (unsigned long long)(pbase + totP) > scr - half) { s.err = 1; pbase = -1; }
+    if (totP > 0) {
+      void* p = sc_up(s, base, half, (unsigned long long)totP * sizeof(PieceRec));
+      rbase = (unsigned long long)p;
+      if (!p) pbase = -1;
+    }
     if (totO + totC > 0 && pbase >= 0) {
       void* p = sc_up(s, base, half, (unsigned long long)(totO + totC) * 4);
-      obase = p ? (unsigned long long)((char*)p - base) : 0;
+      obase = (unsigned long long)p;
       if (!p) pbase = -1;
     }
   }
   pbase = __shfl_sync(0xffffffffu, pbase, 0);
   obase = __shfl_sync(0xffffffffu, obase, 0);
+  rbase = __shfl_sync(0xffffffffu, rbase, 0);
   if (pbase < 0) return;
-  int* olist = (int*)(base + obase);  // open pieces, then continuation pieces, each in y order
+  PieceRec* recs = (PieceRec*)rbase;
+  int* olist = (int*)obase;  // open pieces, then continuation pieces, each in y order
   TSTEP(3)
 
   // ---- write pieces
@@ -421,7 +436,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         pr.z = (rowbase + r) | (int)((hr >> 15) << 17);
         pr.w = rowbase + rend;
         if (!cont) ++h;
-        *rec_at(base, scr, p) = pr;
+        recs[p - pbase] = pr;
         if (open) olist[o++] = p;
         if (cont) olist[totO + q++] = p;
         ++p;
@@ -431,7 +446,9 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   }
   TSTEP(4)
   if (lane == 0) {
-    s.sbinfo[sb] = make_int4(pbase, totP, (int)obase, totO);
+    s.sbinfo[sb] = make_int4(pbase, totP, totO, 0);
+    s.sbol[sb] = (int*)obase;
+    s.sbrec[sb] = recs;
     s.sbh[sb] = totH;
     s.sbct[sb] = totC;
   }
@@ -453,6 +470,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
   for (;;) {
     __syncthreads();
     if (tid == 0) {
+      s.st = st;
       s.tile = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
       s.nA = s.nB = 0;
       s.up = 0;
@@ -572,6 +590,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       s.sbinfo = (int4*)sc_up(s, base, half, (unsigned long long)nsb * 16);
       s.sbh = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
       s.sbct = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
+      s.sbol = (int**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
+      s.sbrec = (PieceRec**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
       s.biglb = nwy > TK_LBW ? (unsigned*)sc_up(s, base, half, (unsigned long long)TK_NW * 2 * nwy * 4)
                              : nullptr;
     }
@@ -621,8 +641,14 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     int* succ = prs ? reinterpret_cast<int*>(s.dbuf + (size_t)NP * 16) : s.succ;
     const int* Xv = xys ? s.xyv : s.Xt;
     const int* Yv = xys ? s.xyv + Nx : s.Yt;
+    // record of global piece q, which belongs to sub-band sb
+    auto REC = [&](int sb, int q) -> PieceRec { return prs ? PR[q] : s.sbrec[sb][q - s.sbinfo[sb].x]; };
+    const int wid = gb_warp(), lane = gb_lane();
     if (prs)
-      for (int p = tid; p < NP; p += TK_NT) PR[p] = *rec_at(base, scr, p);
+      for (int sb = wid; sb < nsb; sb += TK_NW) {
+        const int4 inf = s.sbinfo[sb];
+        for (int j = lane; j < inf.y; j += 32) PR[inf.x + j] = s.sbrec[sb][j];
+      }
     if (xys) {
       for (int i = tid; i < Nx; i += TK_NT) s.xyv[i] = s.Xt[i];
       for (int i = tid; i < Ny; i += TK_NT) s.xyv[Nx + i] = s.Yt[i];
@@ -644,23 +670,27 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     __syncthreads();
     // link every continuation piece to the open piece of the previous
     // sub-band with the same y-interval (open lists are in y order)
-    for (int p = tid; p < NP; p += TK_NT) {
-      const PieceRec pr = prs ? PR[p] : *rec_at(base, scr, p);
-      if (!pr_cont(pr)) continue;
-      const int sbp = pr_slo(pr) / 63 - 1;
-      const int4 inf = s.sbinfo[sbp];
-      const int* ol = (const int*)(base + inf.z);
-      const int y = pr_ylo(pr);
-      int lo = 0, hi = inf.w - 1, q = -1;
-      while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        const int cand = ol[mid];
-        const int yc = pr_ylo(prs ? PR[cand] : *rec_at(base, scr, cand));
-        if (yc == y) { q = cand; break; }
-        if (yc < y) lo = mid + 1; else hi = mid - 1;
+    for (int sb = 1 + wid; sb < nsb; sb += TK_NW) {
+      const int4 inf = s.sbinfo[sb];
+      const int nc = s.sbct[sb];
+      if (!nc) continue;
+      const int* cl = s.sbol[sb] + inf.z;
+      const int4 pinf = s.sbinfo[sb - 1];
+      const int* ol = s.sbol[sb - 1];
+      for (int k = lane; k < nc; k += 32) {
+        const int p = cl[k];
+        const int y = pr_ylo(REC(sb, p));
+        int lo = 0, hi = pinf.z - 1, q = -1;
+        while (lo <= hi) {
+          const int mid = (lo + hi) >> 1;
+          const int cand = ol[mid];
+          const int yc = pr_ylo(REC(sb - 1, cand));
+          if (yc == y) { q = cand; break; }
+          if (yc < y) lo = mid + 1; else hi = mid - 1;
+        }
+        if (q >= 0) succ[q] = p;
+        else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
       }
-      if (q >= 0) succ[q] = p;
-      else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
     }
     __syncthreads();
     if (tid == 0) {
@@ -681,17 +711,21 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     const long long obase = s.obase;
     unsigned long long* outp = obase >= 0 ? O->pcs + obase : nullptr;
     long long area = 0;
-    for (int p = tid; p < NP; p += TK_NT) {
-      const PieceRec pr = prs ? PR[p] : *rec_at(base, scr, p);
-      if (pr_cont(pr)) continue;
-      int q = p, guard = 0;
-      while (succ[q] >= 0 && guard++ <= nsb) q = succ[q];
-      const int shi = q == p ? pr_shi(pr) : pr_shi(prs ? PR[q] : *rec_at(base, scr, q));
-      const int slo = pr_slo(pr);
-      const int xs = Xv[slo], xe = Xv[shi], ylo = Yv[pr_ylo(pr)], yhi = Yv[pr_yhi(pr)];
-      const int pos = s.sbh[slo / 63] + pr_hrank(pr);
-      if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
-      area += (long long)(xe - xs) * (long long)(yhi - ylo);
+    for (int sb = wid; sb < nsb; sb += TK_NW) {
+      const int4 inf = s.sbinfo[sb];
+      for (int j = lane; j < inf.y; j += 32) {
+        const int p = inf.x + j;
+        const PieceRec pr = REC(sb, p);
+        if (pr_cont(pr)) continue;
+        int q = p, sq = sb, guard = 0;
+        while (succ[q] >= 0 && guard++ <= nsb) { q = succ[q]; ++sq; }
+        const int shi = q == p ? pr_shi(pr) : pr_shi(REC(sq, q));
+        const int slo = pr_slo(pr);
+        const int xs = Xv[slo], xe = Xv[shi], ylo = Yv[pr_ylo(pr)], yhi = Yv[pr_yhi(pr)];
+        const int pos = s.sbh[sb] + pr_hrank(pr);
+        if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
+        area += (long long)(xe - xs) * (long long)(yhi - ylo);
+      }
     }
     area = gb_block_sum(area, s.tmp64);
     if (tid == 0) {
