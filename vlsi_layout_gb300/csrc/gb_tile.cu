@@ -42,6 +42,9 @@
 #define TK_NT (TK_NW * 32)
 #define TK_WMAX 2049
 #define TK_NSBMAX 1042
+#define TK_SBS 256
+#define TK_MDS 128   // sub-bands whose metadata fits in the bitmap region after phase B
+#define TK_MD_INTS (TK_MDS * 4 + (TK_MDS + 2) * 2 + TK_MDS * 2 * 2)  // sbinfo, sbh, sbct, sbol, sbrec
 #define TK_LBW 128
 #define TK_LVN 256
 #define TK_LCN 128
@@ -68,11 +71,11 @@ struct TileSmem {
   union {  // phases A-B: value bitmaps and their prefix popcounts; phase D: x / y value tables
     struct {
       unsigned xb[TK_WMAX], yb[TK_WMAX];
-      unsigned xp[TK_WMAX / 4 + 1], yp[TK_WMAX / 4 + 1];  // prefix popcount per 4 words
+      unsigned xp[TK_WMAX / 2 + 1], yp[TK_WMAX / 2 + 1];  // prefix popcount per 2 words
     };
-    int xyv[2 * TK_WMAX + 2 * (TK_WMAX / 4 + 1)];
+    int xyv[2 * TK_WMAX + 2 * (TK_WMAX / 2 + 1)];  // phase D; after the metadata below when it is here
   };
-  int sbc[TK_NSBMAX + 2];
+  int sbc_s[TK_SBS + 2];  // per sub-band member counts / cursors (scratch when more sub-bands)
   union {  // phase C: per-warp sweep buffers; phase D: piece records and chain links
     struct {
       unsigned lb[TK_NW][TK_LBW];
@@ -101,6 +104,7 @@ struct TileSmem {
   int4* sbinfo;  // per sub-band: piece base, piece count, open-list byte offset, open count
   int* sbh;      // heads per sub-band, then their exclusive scan
   int* sbct;     // continuation pieces per sub-band
+  int* sbc;      // per sub-band member counts / cursors (sbc_s or scratch)
   int** sbol;    // open list (then continuation list) per sub-band
   PieceRec** sbrec;  // strip pieces per sub-band (global piece index = sbinfo.x + local index)
   unsigned* biglb;
@@ -120,11 +124,10 @@ __device__ __forceinline__ int bm_rank(const unsigned* bits, const unsigned* pre
   const int w = v >> 5;
   return (int)pref[w] + __popc(bits[w] & ((1u << (v & 31)) - 1u));
 }
-// rank with a prefix stored once per 4 words
-__device__ __forceinline__ int bm_rank4(const unsigned* bits, const unsigned* pref4, int v) {
-  const int w = v >> 5, w0 = w & ~3;
-  int r = (int)pref4[w >> 2];
-  for (int k = w0; k < w; ++k) r += __popc(bits[k]);
+// rank with a prefix stored once per 2 words
+__device__ __forceinline__ int bm_rank2(const unsigned* bits, const unsigned* pref2, int v) {
+  const int w = v >> 5;
+  int r = (int)pref2[w >> 1] + ((w & 1) ? __popc(bits[w - 1]) : 0);
   return r + __popc(bits[w] & ((1u << (v & 31)) - 1u));
 }
 
@@ -348,7 +351,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   TSTEP(2)
 
   // ---- count pieces / opens / heads
-  int np = 0, no = 0, nh = 0, ncn = 0;
+  int np = 0, no = 0, nh = 0, ncn = 0, nz = 0;
   {
     unsigned long long Rm1 = R(c0 - 1), F = Fin;
     for (int c = c0; c < c1e; ++c) {
@@ -365,10 +368,14 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       const int cont = (sb > 0) && ((Z >> 1) & 1ull) && !((Chg >> 1) & 1ull);
       nh += pc - cont;
       ncn += cont;
+      nz += (int)(Ec & 1ull);
       Rm1 = Rc;
     }
   }
-  int totP, totO, totH, totC;
+  int totP, totO, totH, totC, totZ;
+  // runs at row 0 are the runs at row 63 of the previous sub-band, both in y
+  // order: a continuation's ordinal among them indexes that sub-band's open list
+  const int posZ = gb_warp_excl(nz, &totZ);
   const int posP = gb_warp_excl(np, &totP);
   const int posO = gb_warp_excl(no, &totO);
   const int posH = gb_warp_excl(nh, &totH);
@@ -399,7 +406,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   // ---- write pieces
   {
     unsigned long long Rm1 = R(c0 - 1), F = Fin;
-    int p = pbase + posP, o = posO, h = posH, q = posC;
+    int p = pbase + posP, o = posO, h = posH, q = posC, z = posZ;
     for (int c = c0; c < c1e; ++c) {
       const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
       const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
@@ -430,7 +437,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         const int cont = (sb > 0) && (r == 1) && !((Chg >> 1) & 1ull);
         const int open = (rend == 64) && !last_sb;
         PieceRec pr;
-        const unsigned hr = cont ? 0u : (unsigned)h;
+        const unsigned hr = cont ? (unsigned)z : (unsigned)h;  // continuations keep their row-0 ordinal
         pr.x = lv[cs] | (cont << 30) | (open << 31);
         pr.y = lv[c + 1] | (int)((hr & 0x7fffu) << 17);
         pr.z = (rowbase + r) | (int)((hr >> 15) << 17);
@@ -441,6 +448,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         if (cont) olist[totO + q++] = p;
         ++p;
       }
+      z += (int)(Ec & 1ull);
       Rm1 = Rc;
     }
   }
@@ -530,7 +538,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       const long long ex = gb_block_excl(cx | (cy << 32), s.tmp64, &tot);
       unsigned ox = (unsigned)(ex & 0xffffffffll), oy = (unsigned)(ex >> 32);
       for (int w = w0; w < w1; ++w) {
-        if ((w & 3) == 0) { s.xp[w >> 2] = ox; s.yp[w >> 2] = oy; }
+        if ((w & 1) == 0) { s.xp[w >> 1] = ox; s.yp[w >> 1] = oy; }
         ox += __popc(s.xb[w]);
         oy += __popc(s.yb[w]);
       }
@@ -543,7 +551,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       __syncthreads();
       if (!s.err) {
-        int kx = w0 < W ? (int)s.xp[w0 >> 2] : 0, ky = w0 < W ? (int)s.yp[w0 >> 2] : 0;
+        int kx = w0 < W ? (int)s.xp[w0 >> 1] : 0, ky = w0 < W ? (int)s.yp[w0 >> 1] : 0;
         for (int w = w0; w < w1; ++w) {
           unsigned bits = s.xb[w];
           while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Xt[kx++] = (w << 5) + b; }
@@ -556,15 +564,18 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     const int nsb = (nslab + 62) / 63;
     if (timing) { __syncthreads(); const long long t1 = clock64(); tA += t1 - t0; t0 = t1; }
     // ---- B: sub-band membership (counting sort in shared memory)
-    for (int i = tid; i <= nsb; i += TK_NT) s.sbc[i] = 0;
+    if (tid == 0) s.sbc = nsb <= TK_SBS ? s.sbc_s : (int*)sc_up(s, base, half, (unsigned long long)(nsb + 2) * 4);
+    __syncthreads();
+    if (!s.sbc) s.sbc = s.sbc_s;  // only after an error (s.err set); the tile is then abandoned
+    for (int i = tid; i <= min(nsb, s.sbc == s.sbc_s ? TK_SBS : nsb); i += TK_NT) s.sbc[i] = 0;
     __syncthreads();
     if (!s.err) {
       for (int i = tid; i < P; i += TK_NT) {
         const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
         int x1, y1, x2, y2;
         gb_unpack(pk, x1, y1, x2, y2);
-        const int r1 = bm_rank4(s.xb, s.xp, x1), r2 = bm_rank4(s.xb, s.xp, x2);
-        const int c1 = bm_rank4(s.yb, s.yp, y1), c2 = bm_rank4(s.yb, s.yp, y2);
+        const int r1 = bm_rank2(s.xb, s.xp, x1), r2 = bm_rank2(s.xb, s.xp, x2);
+        const int c1 = bm_rank2(s.yb, s.yp, y1), c2 = bm_rank2(s.yb, s.yp, y2);
         s.rk[i] = make_int4(r1, r2, c1, c2);
         const int lo = r1 / 63, hi = min(nsb - 1, r2 / 63);
         for (int q = lo; q <= hi; ++q) atomicAdd(&s.sbc[q], 1);
@@ -574,12 +585,13 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     int M = 0;
     {
       long long carry = 0;
-      for (int b0 = 0; b0 < nsb; b0 += TK_NT) {
+      const int nsbv = s.err ? 0 : nsb;  // after an error the counters are not valid
+      for (int b0 = 0; b0 < nsbv; b0 += TK_NT) {
         const int q = b0 + tid;
-        const long long v = q < nsb ? s.sbc[q] : 0;
+        const long long v = q < nsbv ? s.sbc[q] : 0;
         long long tot;
         const long long ex = gb_block_excl(v, s.tmp64, &tot);
-        if (q < nsb) s.sbc[q] = (int)(carry + ex);
+        if (q < nsbv) s.sbc[q] = (int)(carry + ex);
         carry += tot;
       }
       M = (int)carry;
@@ -587,11 +599,20 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     if (tid == 0) {
       const int nwy = ((Ny - 1) >> 5) + 1;
       s.mem = (int4*)sc_up(s, base, half, (unsigned long long)M * 16);
-      s.sbinfo = (int4*)sc_up(s, base, half, (unsigned long long)nsb * 16);
-      s.sbh = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
-      s.sbct = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
-      s.sbol = (int**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
-      s.sbrec = (PieceRec**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
+      if (nsb <= TK_MDS) {  // the value bitmaps are dead now: keep the metadata on chip
+        char* q = reinterpret_cast<char*>(s.xyv);
+        s.sbinfo = (int4*)q; q += TK_MDS * 16;
+        s.sbol = (int**)q; q += TK_MDS * 8;
+        s.sbrec = (PieceRec**)q; q += TK_MDS * 8;
+        s.sbh = (int*)q; q += (TK_MDS + 2) * 4;
+        s.sbct = (int*)q;
+      } else {
+        s.sbinfo = (int4*)sc_up(s, base, half, (unsigned long long)nsb * 16);
+        s.sbh = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
+        s.sbct = (int*)sc_up(s, base, half, (unsigned long long)nsb * 4 + 4);
+        s.sbol = (int**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
+        s.sbrec = (PieceRec**)sc_up(s, base, half, (unsigned long long)nsb * 8 + 8);
+      }
       s.biglb = nwy > TK_LBW ? (unsigned*)sc_up(s, base, half, (unsigned long long)TK_NW * 2 * nwy * 4)
                              : nullptr;
     }
@@ -626,7 +647,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     constexpr int DBYTES = (int)(sizeof(s.lb) + sizeof(s.lp) + sizeof(s.lv) + sizeof(s.ca) + sizeof(s.cb) +
                                  sizeof(s.mc) + sizeof(s.srow));
     const bool prs = (long long)NP * 20 <= DBYTES;
-    const bool xys = Nx + Ny <= 2 * TK_WMAX + 2 * (TK_WMAX / 4 + 1);
+    const int xyoff = nsb <= TK_MDS ? TK_MD_INTS : 0;  // metadata occupies the front of the region
+    const bool xys = Nx + Ny + xyoff <= 2 * TK_WMAX + 2 * (TK_WMAX / 2 + 1);
     if (tid == 0 && !s.err && !prs) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
     __syncthreads();
     if (s.err) {
@@ -639,8 +661,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     PieceRec* PR = prs ? reinterpret_cast<PieceRec*>(s.dbuf) : nullptr;
     int* succ = prs ? reinterpret_cast<int*>(s.dbuf + (size_t)NP * 16) : s.succ;
-    const int* Xv = xys ? s.xyv : s.Xt;
-    const int* Yv = xys ? s.xyv + Nx : s.Yt;
+    const int* Xv = xys ? s.xyv + xyoff : s.Xt;
+    const int* Yv = xys ? s.xyv + xyoff + Nx : s.Yt;
     // record of global piece q, which belongs to sub-band sb
     auto REC = [&](int sb, int q) -> PieceRec { return prs ? PR[q] : s.sbrec[sb][q - s.sbinfo[sb].x]; };
     const int wid = gb_warp(), lane = gb_lane();
@@ -650,8 +672,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         for (int j = lane; j < inf.y; j += 32) PR[inf.x + j] = s.sbrec[sb][j];
       }
     if (xys) {
-      for (int i = tid; i < Nx; i += TK_NT) s.xyv[i] = s.Xt[i];
-      for (int i = tid; i < Ny; i += TK_NT) s.xyv[Nx + i] = s.Yt[i];
+      for (int i = tid; i < Nx; i += TK_NT) s.xyv[xyoff + i] = s.Xt[i];
+      for (int i = tid; i < Ny; i += TK_NT) s.xyv[xyoff + Nx + i] = s.Yt[i];
     }
     for (int p = tid; p < NP; p += TK_NT) succ[p] = -1;
     int H = 0;
@@ -669,26 +691,17 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     __syncthreads();
     // link every continuation piece to the open piece of the previous
-    // sub-band with the same y-interval (open lists are in y order)
+    // sub-band: its row-0 ordinal indexes that sub-band's open list directly
     for (int sb = 1 + wid; sb < nsb; sb += TK_NW) {
-      const int4 inf = s.sbinfo[sb];
       const int nc = s.sbct[sb];
       if (!nc) continue;
-      const int* cl = s.sbol[sb] + inf.z;
+      const int* cl = s.sbol[sb] + s.sbinfo[sb].z;
       const int4 pinf = s.sbinfo[sb - 1];
       const int* ol = s.sbol[sb - 1];
       for (int k = lane; k < nc; k += 32) {
         const int p = cl[k];
-        const int y = pr_ylo(REC(sb, p));
-        int lo = 0, hi = pinf.z - 1, q = -1;
-        while (lo <= hi) {
-          const int mid = (lo + hi) >> 1;
-          const int cand = ol[mid];
-          const int yc = pr_ylo(REC(sb - 1, cand));
-          if (yc == y) { q = cand; break; }
-          if (yc < y) lo = mid + 1; else hi = mid - 1;
-        }
-        if (q >= 0) succ[q] = p;
+        const int ord = pr_hrank(REC(sb, p));
+        if (ord < pinf.z) succ[ol[ord]] = p;
         else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
       }
     }
