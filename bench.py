@@ -178,6 +178,59 @@ def serve_leg(rates=(1000, 10000), seconds=0.5, max_req=3000, seed=4, slots=8):
     return out
 
 
+def sort_leg(n=200_000_000, steps=5, seed=5):
+    """Device-resident Morton sort of n boxes (the BuildTree / SortBoxesDirect
+    step): Morton keys of a cfg3-sized die, then the onesweep radix sort.
+    Algorithmic bytes per sort = n*8 (histogram read) + passes * n * 2 * (8+4)."""
+    import torch
+    from vlsi_layout_gb300 import engine
+    L = engine.lib()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    die = 40_000_000
+    x = torch.randint(0, die - 2000, (n,), device="cuda", generator=g, dtype=torch.int32)
+    y = torch.randint(0, die - 2000, (n,), device="cuda", generator=g, dtype=torch.int32)
+    w = torch.randint(20, 2001, (n,), device="cuda", generator=g, dtype=torch.int32)
+    boxes = torch.stack([x, y, x + w, y + w], 1).contiguous()
+    del x, y, w
+    keys = torch.empty(n, dtype=torch.int64, device="cuda")
+    vals = torch.empty(n, dtype=torch.int32, device="cuda")
+    kt = torch.empty_like(keys)
+    vt = torch.empty_like(vals)
+    stream = torch.cuda.current_stream()
+    with engine.Context(0) as ctx:
+        ctx.set_stream(stream.cuda_stream) if stream.cuda_stream else None
+        k0 = torch.empty_like(keys)
+        v0 = torch.empty_like(vals)
+        L.gb_morton_keys_device(ctx.h, boxes.data_ptr(), n, k0.data_ptr(), v0.data_ptr())
+        span = int((k0 ^ k0[0]).max().item()) if n > 1 else 0
+        bits = max(1, span.bit_length())
+        times = []
+        for it in range(steps + 1):
+            keys.copy_(k0)
+            vals.copy_(v0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            passes = L.gb_radix_sort_device(ctx.h, keys.data_ptr(), vals.data_ptr(), n, bits, kt.data_ptr(),
+                                            vt.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if it:
+                times.append(e0.elapsed_time(e1))
+        ctx.sync()
+        ok = bool((keys[1:] >= keys[:-1]).all().item()) if False else None
+        ks = keys.view(torch.int64)
+        # keys are below 2^63 here (bit 63 of the Morton code is y's sign bit, constant for this die)
+        sorted_ok = bool((ks[1:] >= ks[:-1]).all().item())
+    ms = statistics.median(times)
+    byts = n * 8 + passes * n * 2 * 12
+    peak, kind = peaks()
+    return {"n": n, "bits": bits, "passes": passes, "ms": ms, "keys_per_s": n / (ms / 1e3),
+            "gb_s": byts / (ms / 1e3) / 1e9, "frac_of_peak": byts / (ms / 1e3) / 1e9 / peak,
+            "peak": peak, "sorted": sorted_ok}
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -240,8 +293,14 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--serve-rates", default="1000,10000")
+    ap.add_argument("--sort-only", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
+    if args.sort_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"sort": sort_leg()}), flush=True)
+        return
     if args.serve_only:
         import torch
         torch.cuda.set_device(local)

@@ -164,6 +164,17 @@ int gb_components(gb_context* ctx, const c_box* boxes, unsigned long long n, lon
 int gb_morton_sort(gb_context* ctx, c_box* boxes, long long n, int sort_boxes,
                    unsigned long long* keys_out, long long* perm);
 
+/* Device-resident LSD radix sort of (key, value) pairs by the low `bits`
+ * key bits, 8-bit digits, stable; the *_tmp buffers hold n entries.  The
+ * sorted pairs end in d_keys / d_vals.  Returns the number of passes (>= 0)
+ * or a negative status.  Asynchronous on the context stream. */
+int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n, int bits,
+                         unsigned long long* d_keys_tmp, unsigned* d_vals_tmp);
+/* Morton keys of device boxes (gpu_morton.cu:113-144) and the identity
+ * permutation, on the device. */
+int gb_morton_keys_device(gb_context* ctx, const c_box* d_boxes, long long n, unsigned long long* d_keys,
+                          unsigned* d_vals);
+
 /* Canonical order: sort n host boxes by (x1, y1, x2, y2). */
 int gb_canonical_sort(gb_context* ctx, c_box* boxes, long long n);
 

@@ -837,6 +837,21 @@ extern "C" int gb_canonical_sort(gb_context* ctx, c_box* boxes, long long n) {
 
 extern "C" int32_t gb_um_to_dbu(double r) { return (int32_t)(1000.0 * r); }
 
+extern "C" int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n,
+                                    int bits, unsigned long long* d_keys_tmp, unsigned* d_vals_tmp) {
+  if (!ctx || n < 0 || bits < 1 || bits > 64 || (n > 1 && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp)))
+    return GB_ERR_ARG;
+  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp, 8);
+  return p < 0 ? set_err(ctx, GB_ERR_INTERNAL, "radix sort setup failed") : p;
+}
+
+extern "C" int gb_morton_keys_device(gb_context* ctx, const c_box* d_boxes, long long n, unsigned long long* d_keys,
+                                     unsigned* d_vals) {
+  if (!ctx || n < 0 || (n > 0 && (!d_boxes || !d_keys || !d_vals))) return GB_ERR_ARG;
+  k_morton_keys<<<ctx->c.work_blocks, 256, 0, ctx->c.stream>>>((const int4*)d_boxes, n, d_keys, d_vals);
+  return GB_OK;
+}
+
 // ======================================================================= drop-ins
 static int host_bool(gb_context* ctx, int control, long value, const c_box* A, unsigned long AN,
                      const c_box* B, unsigned long BN, std::vector<c_box>& res) {

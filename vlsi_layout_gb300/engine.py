@@ -91,6 +91,8 @@ def lib():
         "gb_launch_count": (i64, [P]),
         "gb_run_deck": (ctypes.c_int, [ctypes.c_char_p, P, u64, P]),
         "gb_debug_lookback_timeout": (ctypes.c_int, [P, ctypes.c_int]),
+        "gb_radix_sort_device": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P]),
+        "gb_morton_keys_device": (ctypes.c_int, [P, P, i64, P, P]),
         "gb_serve_create": (ctypes.c_int, [ctypes.c_int, u64, ctypes.c_int, u64, pp]),
         "gb_serve_add_layer": (ctypes.c_int, [P, P, u64, P]),
         "gb_serve_run": (ctypes.c_int, [P, P, ctypes.c_int, P, ctypes.c_int]),
