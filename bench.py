@@ -178,9 +178,10 @@ def serve_leg(rates=(1000, 10000), seconds=0.5, max_req=3000, seed=4, slots=8):
     return out
 
 
-def sort_leg(n=200_000_000, steps=5, seed=5):
+def sort_leg(n=200_000_000, steps=5, seed=5, tune=True):
     """Device-resident Morton sort of n boxes (the BuildTree / SortBoxesDirect
-    step): Morton keys of a cfg3-sized die, then the onesweep radix sort.
+    step): Morton keys of a 4e7 x 4e7 dbu die, then the onesweep radix sort,
+    first in its default configuration, then in the one the autotuner picks.
     Algorithmic bytes per sort = n*8 (histogram read) + passes * n * 2 * (8+4)."""
     import torch
     from vlsi_layout_gb300 import engine
@@ -198,37 +199,54 @@ def sort_leg(n=200_000_000, steps=5, seed=5):
     vt = torch.empty_like(vals)
     stream = torch.cuda.Stream()  # a real stream shared by the engine, the copies and the events
     torch.cuda.set_stream(stream)
+    peak, kind = peaks()
+    out = {"n": n, "peak": peak}
     with engine.Context(0) as ctx:
         ctx.set_stream(stream.cuda_stream)
         k0 = torch.empty_like(keys)
         v0 = torch.empty_like(vals)
         L.gb_morton_keys_device(ctx.h, boxes.data_ptr(), n, k0.data_ptr(), v0.data_ptr())
+        del boxes
         span = int((k0 ^ k0[0]).max().item()) if n > 1 else 0
         bits = max(1, span.bit_length())
-        times = []
-        for it in range(steps + 1):
-            keys.copy_(k0)
-            vals.copy_(v0)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            passes = L.gb_radix_sort_device(ctx.h, keys.data_ptr(), vals.data_ptr(), n, bits, kt.data_ptr(),
-                                            vt.data_ptr())
-            e1.record(stream)
-            torch.cuda.synchronize()
-            if it:
-                times.append(e0.elapsed_time(e1))
-        ctx.sync()
-        ks = keys.view(torch.int64)
-        # keys are below 2^63 here (bit 63 of the Morton code is y's sign bit, constant for this die)
-        sorted_ok = bool((ks[1:] >= ks[:-1]).all().item())
-    ms = statistics.median(times)
-    byts = n * 8 + passes * n * 2 * 12
-    peak, kind = peaks()
-    return {"n": n, "bits": bits, "passes": passes, "ms": ms, "keys_per_s": n / (ms / 1e3),
-            "gb_s": byts / (ms / 1e3) / 1e9, "frac_of_peak": byts / (ms / 1e3) / 1e9 / peak,
-            "peak": peak, "sorted": sorted_ok}
+        out["bits"] = bits
+
+        def timed(label):
+            times = []
+            passes = 0
+            for it in range(steps + 1):
+                keys.copy_(k0)
+                vals.copy_(v0)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                passes = ctx.radix_sort_device(keys.data_ptr(), vals.data_ptr(), n, bits, kt.data_ptr(),
+                                               vt.data_ptr())
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if it:
+                    times.append(e0.elapsed_time(e1))
+            ctx.sync()
+            ks = keys.view(torch.int64)
+            # keys are below 2^63 here (bit 63 of the Morton code is y's sign bit, constant for this die)
+            sorted_ok = bool((ks[1:] >= ks[:-1]).all().item())
+            ms = statistics.median(times)
+            byts = n * 8 + passes * n * 2 * 12
+            out[label] = {"passes": passes, "ms": ms, "keys_per_s": n / (ms / 1e3),
+                          "gb_s": byts / (ms / 1e3) / 1e9, "frac_of_peak": byts / (ms / 1e3) / 1e9 / peak,
+                          "sorted": sorted_ok}
+
+        L.gb_radix_tuning_reset()
+        timed("default")
+        if tune:
+            p, items, tms = ctx.radix_autotune(k0.data_ptr(), v0.data_ptr(), n, bits)
+            timed("tuned")
+            out["tuned"]["items_per_thread"] = items
+            L.gb_radix_tuning_reset()
+    best = min((out[k] for k in ("default", "tuned") if k in out), key=lambda r: r["ms"])
+    out.update({k: best[k] for k in ("passes", "ms", "keys_per_s", "gb_s", "frac_of_peak", "sorted")})
+    return out
 
 
 def dist_init():
@@ -294,12 +312,13 @@ def main():
     ap.add_argument("--serve-only", action="store_true")
     ap.add_argument("--serve-rates", default="1000,10000")
     ap.add_argument("--sort-only", action="store_true")
+    ap.add_argument("--sort-n", type=int, default=200_000_000)
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
     if args.sort_only:
         import torch
         torch.cuda.set_device(local)
-        print(json.dumps({"sort": sort_leg()}), flush=True)
+        print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps)}), flush=True)
         return
     if args.serve_only:
         import torch

@@ -321,6 +321,7 @@ extern "C" int gb_context_destroy(gb_context* ctx) {
   cudaFree(c.tile_counter);
   cudaFree(c.desc);
   cudaFree(c.tile_scratch);
+  gb_radix_free(c);
   if (c.own_stream) cudaStreamDestroy(c.stream);
   if (ctx == g_default) g_default = nullptr;
   delete ctx;
@@ -733,7 +734,7 @@ static int sort_keys_perm(gb_context* ctx, unsigned long long* dkeys, unsigned* 
     if (kt) cudaFree(kt);
     return set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in sort");
   }
-  int p = gb_radix_sort_pairs(c, dkeys, dvals, n, bits, kt, vt, 8);
+  int p = gb_radix_sort_pairs(c, dkeys, dvals, n, bits, kt, vt);
   cudaStreamSynchronize(c.stream);
   cudaFree(kt);
   cudaFree(vt);
@@ -840,10 +841,32 @@ extern "C" int32_t gb_um_to_dbu(double r) { return (int32_t)(1000.0 * r); }
 extern "C" int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n,
                                     int bits, unsigned long long* d_keys_tmp, unsigned* d_vals_tmp) {
   if (!ctx || n < 0 || bits < 1 || bits > 64 || (n > 1 && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp)))
-    return GB_ERR_ARG;
-  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp, 8);
-  return p < 0 ? set_err(ctx, GB_ERR_INTERNAL, "radix sort setup failed") : p;
+    return -GB_ERR_ARG;
+  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp);
+  if (p == -2) return -set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in radix sort");
+  return p < 0 ? -set_err(ctx, GB_ERR_INTERNAL, "radix sort setup failed") : p;
 }
+
+extern "C" int gb_radix_sort_device_cfg(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n,
+                                        int bits, unsigned long long* d_keys_tmp, unsigned* d_vals_tmp, int passes,
+                                        int items) {
+  if (!ctx || n < 0 || bits < 1 || bits > 64 || (n > 1 && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp)))
+    return -GB_ERR_ARG;
+  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp, passes, items);
+  if (p == -2) return -set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in radix sort");
+  return p < 0 ? -set_err(ctx, GB_ERR_ARG, "radix sort configuration not available") : p;
+}
+
+extern "C" int gb_radix_autotune(gb_context* ctx, const unsigned long long* d_keys, const unsigned* d_vals,
+                                 long long n, int bits, int* passes, int* items, float* ms) {
+  if (!ctx || n < 2 || bits < 1 || bits > 64 || !d_keys || !d_vals) return GB_ERR_ARG;
+  const int r = gb_radix_tune(ctx->c, d_keys, d_vals, n, bits, passes, items, ms);
+  if (r == -2) return set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in radix autotune");
+  if (r < 0) return set_err(ctx, GB_ERR_INTERNAL, "radix autotune found no configuration");
+  return gb_sync(ctx, nullptr);
+}
+
+extern "C" void gb_radix_tuning_reset(void) { gb_radix_forget_tuning(); }
 
 extern "C" int gb_morton_keys_device(gb_context* ctx, const c_box* d_boxes, long long n, unsigned long long* d_keys,
                                      unsigned* d_vals) {

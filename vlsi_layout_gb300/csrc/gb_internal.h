@@ -41,6 +41,7 @@ struct GbCtx {
   unsigned prof_flags = 0;
   bool timing = false;               // per-phase clock64 counters in the tile kernel
   long long launches = 0;            // kernels issued by the engine (host-side count)
+  void* rs = nullptr;                // radix sort state (histograms, look-back status), gb_radix.cu
 };
 
 struct gb_layer {
@@ -122,9 +123,16 @@ void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* pare
 
 // ---- radix sort (gb_radix.cu)
 // Sorts n (key, value) pairs by the low `bits` bits of the 64-bit keys.
-// tmp buffers must hold n entries each.  Stable.
+// tmp buffers must hold n entries each.  Stable.  passes / items (keys per
+// thread: 8, 12, 16 or 20) <= 0 take the tuned or default choice.  Returns
+// the pass count, or < 0 when the configuration is not available.
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
-                        unsigned long long* keys_tmp, unsigned* vals_tmp, int digit_bits);
+                        unsigned long long* keys_tmp, unsigned* vals_tmp, int passes = 0, int items = 0);
+int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals, long long n, int bits,
+                      int* best_passes, int* best_items, float* best_ms);
+void gb_radix_default(int bits, int* passes, int* items);
+void gb_radix_forget_tuning();
+void gb_radix_free(GbCtx& c);
 
 int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit);
 

@@ -3,175 +3,386 @@
 // tracker events (event_sorter.cu:48-81) and canonical strip order.
 //
 //  1. One read of the keys builds the digit histograms of every pass
-//     (per-CTA shared-memory counters, merged with global atomics).
+//     (per-CTA shared-memory counters, merged with global atomics; a digit
+//     that is the same across a warp is counted with one atomic).
 //  2. Each pass is one kernel: a CTA takes the next tile from an atomic
-//     counter (so tiles start in order), ranks its keys stably with warp
-//     match/ballot ranking, publishes its per-digit counts, and obtains the
-//     exclusive prefix of all earlier tiles by a decoupled look-back over a
-//     status array.  Keys are staged in shared memory by digit and written
-//     out in runs.
-// Status words carry an epoch tag, so the array is never cleared between
-// passes.  Every look-back wait is bounded: after the limit the kernel flags
+//     counter (so tiles start in order) and pulls the tile's keys and values
+//     into shared memory with two bulk asynchronous copies completing on an
+//     mbarrier.  Warps rank the keys stably with warp match ranking, the CTA
+//     publishes its per-digit counts, and obtains the exclusive prefix of all
+//     earlier tiles by a decoupled look-back over a status array.  Keys and
+//     values are then permuted in place in shared memory by digit and
+//     written out in runs.
+// Digits are 1..10 bits wide; the passes split the significant key bits as
+// evenly as possible (e.g. 52 bits in 6 passes: 9,9,9,9,8,8), so the pass
+// count is a free choice.  An even pass count leaves the result in place;
+// an odd one costs a final copy.
+// Status words ([tile][digit]) carry an epoch tag, so the array is never
+// cleared between passes.  Every wait is bounded: after the limit the kernel flags
 // GB_ERR_TIMEOUT in the context status and finishes without hanging.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "gb_internal.h"
 #include "gb_scan.cuh"
 
 #define RS_THREADS 256
 #define RS_WARPS (RS_THREADS / 32)
-#define RS_IT 16
-#define RS_TILE (RS_THREADS * RS_IT)
-#define RS_RADIX 256
-#define RS_MAXPASS 8
+#define RS_MAXPASS 16
+#define RS_HIST_SLOTS 8192
 #define RS_SPIN_LIMIT (1 << 22)
 #define KID_RADIX 40
+#define KID_RADIX_COPY 41
 
 // status word: [63:48] epoch, [47:46] flag (1 aggregate, 2 inclusive prefix), [45:0] value
 #define RS_FLAG_AGG 1ull
 #define RS_FLAG_PRE 2ull
 
-__global__ void __launch_bounds__(RS_THREADS)
-k_rs_hist(const unsigned long long* __restrict__ keys, long long n, int passes, int dbits,
-          unsigned* __restrict__ ghist) {
-  __shared__ unsigned h[RS_MAXPASS][RS_RADIX];
-  for (int i = threadIdx.x; i < RS_MAXPASS * RS_RADIX; i += blockDim.x) (&h[0][0])[i] = 0;
+struct RsPlan {
+  int np;
+  int shift[RS_MAXPASS];
+  int bits[RS_MAXPASS];
+  int off[RS_MAXPASS];  // offset of the pass's counters in the histogram array
+};
+
+// ---------------------------------------------------------------- histogram
+template <bool V2>
+__global__ void __launch_bounds__(256)
+k_rs_hist(const unsigned long long* __restrict__ keys, long long n, RsPlan plan, unsigned* __restrict__ ghist) {
+  __shared__ unsigned h[RS_HIST_SLOTS];
+  const int tot_slots = plan.off[plan.np - 1] + (1 << plan.bits[plan.np - 1]);
+  for (int i = threadIdx.x; i < tot_slots; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  const unsigned mask = (1u << dbits) - 1u;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long k = keys[i];
-    for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (p * dbits)) & mask], 1u);
+  const int lane = threadIdx.x & 31;
+  const long long step = (long long)gridDim.x * blockDim.x;
+  // items: pairs of keys (V2) or single keys
+  const long long nit = V2 ? (n >> 1) : n;
+  for (long long wb = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); wb < nit; wb += step) {
+    const long long i = wb + lane;
+    const bool ok = i < nit;
+    const unsigned okm = __ballot_sync(0xffffffffu, ok);
+    unsigned long long k0 = 0, k1 = 0;
+    if (ok) {
+      if (V2) {
+        const ulonglong2 v = reinterpret_cast<const ulonglong2*>(keys)[i];
+        k0 = v.x;
+        k1 = v.y;
+      } else {
+        k0 = keys[i];
+        k1 = k0;
+      }
+    }
+    const int first = __ffs(okm) - 1;
+    for (int p = 0; p < plan.np; ++p) {
+      const unsigned m = (1u << plan.bits[p]) - 1u;
+      const unsigned d0 = (unsigned)(k0 >> plan.shift[p]) & m;
+      const unsigned d1 = (unsigned)(k1 >> plan.shift[p]) & m;
+      const unsigned dl = __shfl_sync(0xffffffffu, d0, first);
+      if (__all_sync(0xffffffffu, !ok || (d0 == dl && d1 == dl))) {
+        if (lane == first) atomicAdd(&h[plan.off[p] + dl], (unsigned)__popc(okm) * (V2 ? 2u : 1u));
+      } else if (ok) {
+        atomicAdd(&h[plan.off[p] + d0], 1u);
+        if (V2) atomicAdd(&h[plan.off[p] + d1], 1u);
+      }
+    }
+  }
+  if (V2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long k = keys[n - 1];
+    for (int p = 0; p < plan.np; ++p)
+      atomicAdd(&h[plan.off[p] + ((unsigned)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1u))], 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < passes * RS_RADIX; i += blockDim.x) {
-    const unsigned v = (&h[0][0])[i];
+  for (int i = threadIdx.x; i < tot_slots; i += blockDim.x) {
+    const unsigned v = h[i];
     if (v) atomicAdd(&ghist[i], v);
   }
 }
 
-__global__ void k_rs_hist_scan(unsigned* ghist, int passes, int radix) {
-  // one block of RS_RADIX threads per pass
+// one block of 1024 threads per pass: exclusive scan of the pass's digit counts
+__global__ void __launch_bounds__(1024) k_rs_hist_scan(unsigned* ghist, RsPlan plan) {
   __shared__ long long tmp[33];
   const int p = blockIdx.x;
-  const long long v = threadIdx.x < radix ? ghist[p * RS_RADIX + threadIdx.x] : 0;
+  const int radix = 1 << plan.bits[p];
+  unsigned* g = ghist + plan.off[p];
+  const long long v = threadIdx.x < radix ? g[threadIdx.x] : 0;
   long long tot;
   const long long ex = gb_block_excl(v, tmp, &tot);
-  if (threadIdx.x < radix) ghist[p * RS_RADIX + threadIdx.x] = (unsigned)ex;
+  if (threadIdx.x < radix) g[threadIdx.x] = (unsigned)ex;
 }
 
-struct RsSmem {
-  unsigned long long k[RS_TILE];
-  unsigned v[RS_TILE];
-  unsigned short wh[RS_WARPS][RS_RADIX];  // per-warp digit counts
-  unsigned bstart[RS_RADIX];              // tile-local bucket start
-  unsigned long long gpos[RS_RADIX];      // global start of this tile's run of digit d
-  long long tile;
-};
+// ---------------------------------------------------------------- async copy helpers
+__device__ __forceinline__ unsigned rs_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
-__global__ void __launch_bounds__(RS_THREADS)
+__device__ __forceinline__ void rs_mbar_init(unsigned a) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void rs_mbar_expect(unsigned a, unsigned bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+
+// global -> shared bulk copy; both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void rs_bulk_load(unsigned dst, const void* src, unsigned bytes, unsigned mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool rs_mbar_try(unsigned a, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for phase 0 of the mbarrier; false after `limit` polls
+__device__ __forceinline__ bool rs_mbar_wait(unsigned a, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (rs_mbar_try(a, 0)) return true;
+  return false;
+}
+
+// ---------------------------------------------------------------- one pass
+// Shared memory of a pass with tile T = RS_THREADS * IT keys and radix R:
+//   keys T*8 | vals T*4 | wh[RS_WARPS][R] u16 | bstart[R] u32 | gpos[R] i64 | mbarrier, tile, scan scratch
+__host__ __device__ constexpr size_t rs_smem_bytes(int it, int radix) {
+  return (size_t)RS_THREADS * it * 12 + (size_t)RS_WARPS * radix * 2 + (size_t)radix * 4 + (size_t)radix * 8 +
+         16 + 33 * 8;
+}
+
+__device__ __forceinline__ unsigned rs_digit(unsigned long long k, int shift, unsigned mask) {
+  return (unsigned)(k >> shift) & mask;
+}
+
+template <int IT>
+__global__ void __launch_bounds__(RS_THREADS, IT <= 8 ? 5 : IT <= 16 ? 4 : 3)
 k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict__ vin,
-          unsigned long long* __restrict__ kout, unsigned* __restrict__ vout, long long n, int shift,
-          int dbits, const unsigned* __restrict__ gofs, unsigned long long* status,
-          unsigned long long epoch, long long* counter, DStatus* st, int spin_limit) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  RsSmem& s = *reinterpret_cast<RsSmem*>(smraw);
-  const int lane = gb_lane(), wid = gb_warp();
+          unsigned long long* __restrict__ kout, unsigned* __restrict__ vout, long long n, int shift, int dbits,
+          const unsigned* __restrict__ gofs, unsigned long long* status, unsigned long long epoch,
+          long long* counter, DStatus* st, int spin_limit, int bulk) {
+  constexpr int TILE = RS_THREADS * IT;
+  extern __shared__ __align__(128) unsigned char smraw[];
   const int radix = 1 << dbits;
   const unsigned mask = (unsigned)radix - 1u;
-  const long long ntile = (n + RS_TILE - 1) / RS_TILE;
-  if (threadIdx.x == 0) s.tile = (long long)atomicAdd((unsigned long long*)counter, 1ull);
-  for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += blockDim.x) (&s.wh[0][0])[i] = 0;
+  unsigned long long* sk = reinterpret_cast<unsigned long long*>(smraw);
+  unsigned* sv = reinterpret_cast<unsigned*>(sk + TILE);
+  unsigned short* wh = reinterpret_cast<unsigned short*>(sv + TILE);  // [RS_WARPS][radix]
+  unsigned* bstart = reinterpret_cast<unsigned*>(wh + RS_WARPS * radix);
+  long long* gpos = reinterpret_cast<long long*>(bstart + radix);
+  unsigned long long* mbar = reinterpret_cast<unsigned long long*>(gpos + radix);
+  long long* stile = reinterpret_cast<long long*>(mbar + 1);
+  long long* tmp = stile + 1;  // [33]
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const long long ntile = (n + TILE - 1) / TILE;
+  const unsigned mb = rs_smem(mbar);
+
+  if (tid == 0) {
+    const long long t = (long long)atomicAdd((unsigned long long*)counter, 1ull);
+    *stile = t;
+    if (bulk && t < ntile) {
+      const long long tb = t * TILE;
+      const int cb = (int)min((long long)TILE, n - tb) & ~3;  // bulk part: whole 16-byte groups
+      rs_mbar_init(mb);
+      rs_mbar_expect(mb, (unsigned)cb * 12u);
+      if (cb > 0) {
+        rs_bulk_load(rs_smem(sk), kin + tb, (unsigned)cb * 8u, mb);
+        rs_bulk_load(rs_smem(sv), vin + tb, (unsigned)cb * 4u, mb);
+      }
+    }
+  }
+  for (int i = tid; i < RS_WARPS * radix / 2; i += RS_THREADS) reinterpret_cast<unsigned*>(wh)[i] = 0u;
   __syncthreads();
-  const long long tile = s.tile;
+  const long long tile = *stile;
   if (tile >= ntile) return;
-  const long long tbase = tile * RS_TILE;
-  // ---- load (warp-striped: warp w owns a contiguous range) and rank
-  unsigned long long key[RS_IT];
-  unsigned val[RS_IT];
-  unsigned short rnk[RS_IT];
+  const long long tb = tile * TILE;
+  const int cnt = (int)min((long long)TILE, n - tb);
+  if (bulk) {
+    for (int i = (cnt & ~3) + tid; i < cnt; i += RS_THREADS) {
+      sk[i] = kin[tb + i];
+      sv[i] = vin[tb + i];
+    }
+    const bool ok = rs_mbar_wait(mb, spin_limit);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX_COPY, tile);
+      rs_mbar_wait(mb, spin_limit);  // let copies in flight land before the CTA exits
+      return;
+    }
+  } else {
+    for (int i = tid; i < cnt; i += RS_THREADS) {
+      sk[i] = kin[tb + i];
+      sv[i] = vin[tb + i];
+    }
+    __syncthreads();
+  }
+
+  // ---- rank: warp w owns keys [w*32*IT, (w+1)*32*IT) in order.  Peers with
+  // the same digit are found by a warp match; the lowest peer adds the group
+  // to the warp's counter (two 16-bit counters share a 32-bit word; a count
+  // never exceeds 32*IT, so no carry crosses halves) and broadcasts the old
+  // value.
   const unsigned lt = (1u << lane) - 1u;
+  const int wbase = wid * 32 * IT;
+  unsigned short* mywh = wh + wid * radix;
+  unsigned* mywh32 = reinterpret_cast<unsigned*>(mywh);
+  unsigned rk[(IT + 1) / 2];
 #pragma unroll
-  for (int it = 0; it < RS_IT; ++it) {
-    const long long pos = tbase + (long long)wid * 32 * RS_IT + it * 32 + lane;
-    const bool ok = pos < n;
-    key[it] = ok ? kin[pos] : ~0ull;
-    val[it] = ok ? vin[pos] : 0u;
-    const unsigned d = ok ? (unsigned)((key[it] >> shift) & mask) : 0xFFFFu;
+  for (int it = 0; it < IT; ++it) {
+    const int idx = wbase + it * 32 + lane;
+    const bool ok = idx < cnt;
+    const unsigned d = ok ? rs_digit(sk[idx], shift, mask) : 0xFFFFu;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const unsigned before = s.wh[wid][ok ? d : 0];
-    __syncwarp();
-    rnk[it] = (unsigned short)(before + __popc(peers & lt));
-    if (ok && (peers & lt) == 0) s.wh[wid][d] = (unsigned short)(before + __popc(peers));
-    __syncwarp();
+    const int leader = __ffs(peers) - 1;
+    unsigned old = 0;
+    if (ok && lane == leader) old = atomicAdd(&mywh32[d >> 1], (unsigned)__popc(peers) << ((d & 1u) * 16));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    const unsigned r = ((old >> ((d & 1u) * 16)) & 0xFFFFu) + __popc(peers & lt);
+    if (it & 1) rk[it >> 1] |= r << 16;
+    else rk[it >> 1] = r;
   }
   __syncthreads();
-  // ---- per-digit prefix over warps, tile totals, bucket starts
-  unsigned tot = 0;
-  if (threadIdx.x < radix) {
-    const int d = threadIdx.x;
-    for (int w = 0; w < RS_WARPS; ++w) {
-      const unsigned c = s.wh[w][d];
-      s.wh[w][d] = (unsigned short)tot;
-      tot += c;
+
+  // ---- per digit: offsets over warps, tile total, aggregate published
+  // (loops over a thread's digits run to the compile-time bound 4 so the
+  // per-digit arrays stay in registers)
+  const int dpt = radix > RS_THREADS ? radix / RS_THREADS : 1;  // digits per thread (1..4)
+  const int d0 = tid * dpt;
+  const bool dig = d0 < radix;
+  unsigned tots[4] = {0u, 0u, 0u, 0u};
+  long long tsum = 0;
+  const unsigned long long etag = (epoch & 0xFFFFull) << 48;
+  if (dig) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < dpt) {
+        const int d = d0 + j;
+        unsigned tot = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) {
+          const unsigned c = wh[w * radix + d];
+          wh[w * radix + d] = (unsigned short)tot;
+          tot += c;
+        }
+        tots[j] = tot;
+        tsum += tot;
+        const unsigned long long flag = tile == 0 ? RS_FLAG_PRE : RS_FLAG_AGG;
+        *(volatile unsigned long long*)(status + (size_t)tile * radix + d) = etag | (flag << 46) | tot;
+      }
     }
   }
   {
-    __shared__ long long tmp[33];
     long long tt;
-    const long long ex = gb_block_excl((long long)(threadIdx.x < radix ? tot : 0), tmp, &tt);
-    if (threadIdx.x < radix) s.bstart[threadIdx.x] = (unsigned)ex;
-  }
-  // ---- decoupled look-back (one thread per digit)
-  if (threadIdx.x < radix) {
-    const int d = threadIdx.x;
-    unsigned long long* my = status + (size_t)tile * RS_RADIX + d;
-    const unsigned long long etag = (epoch & 0xFFFFull) << 48;
-    unsigned long long excl = 0;
-    if (tile == 0) {
-      *(volatile unsigned long long*)my = etag | (RS_FLAG_PRE << 46) | (unsigned long long)tot;
-    } else {
-      *(volatile unsigned long long*)my = etag | (RS_FLAG_AGG << 46) | (unsigned long long)tot;
-      long long j = tile - 1;
-      int spins = 0;
-      while (j >= 0) {
-        const unsigned long long w = *(volatile unsigned long long*)(status + (size_t)j * RS_RADIX + d);
-        const unsigned long long flag = (w >> 46) & 3ull;
-        if ((w & 0xFFFF000000000000ull) != etag || flag == 0) {
-          if (++spins > spin_limit) {
-            gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX, j);
-            break;
-          }
-          continue;
-        }
-        excl += w & ((1ull << 46) - 1);
-        if (flag == RS_FLAG_PRE) break;
-        --j;
-      }
-      __threadfence();
-      *(volatile unsigned long long*)my = etag | (RS_FLAG_PRE << 46) | (excl + tot);
-    }
-    s.gpos[d] = (unsigned long long)gofs[d] + excl;
-  }
-  __syncthreads();
-  // ---- stage in shared memory by digit
+    long long ex = gb_block_excl(tsum, tmp, &tt);
+    if (dig) {
 #pragma unroll
-  for (int it = 0; it < RS_IT; ++it) {
-    const long long pos = tbase + (long long)wid * 32 * RS_IT + it * 32 + lane;
-    if (pos < n) {
-      const unsigned d = (unsigned)((key[it] >> shift) & mask);
-      const unsigned lp = s.bstart[d] + s.wh[wid][d] + rnk[it];
-      s.k[lp] = key[it];
-      s.v[lp] = val[it];
+      for (int j = 0; j < 4; ++j) {
+        if (j < dpt) {
+          bstart[d0 + j] = (unsigned)ex;
+          ex += tots[j];
+        }
+      }
+    }
+  }
+  // ---- decoupled look-back: the thread of digit d polls the status words of
+  // DEPTH predecessors at once (a warp reads whole rows of the [tile][digit]
+  // array), sums aggregates up to the nearest inclusive prefix, and polls
+  // again from the first word that was not yet published.
+  if (dig) {
+    constexpr int DEPTH = 8;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < dpt) {
+        const int d = d0 + j;
+        long long excl = 0;
+        if (tile > 0) {
+          long long jp = tile - 1;  // next predecessor to read
+          int spins = 0;
+          const int depth = DEPTH / dpt;
+          for (;;) {
+            unsigned long long w[DEPTH];
+#pragma unroll
+            for (int i = 0; i < DEPTH; ++i)
+              w[i] = (i < depth && jp - i >= 0) ? *(volatile unsigned long long*)(status + (size_t)(jp - i) * radix + d)
+                                               : 0ull;
+            int used = 0;
+            bool fin = false;
+#pragma unroll
+            for (int i = 0; i < DEPTH; ++i) {
+              if (fin || used < i || i >= depth || jp - i < 0) continue;
+              const unsigned long long fl = (w[i] >> 46) & 3ull;
+              if ((w[i] & 0xFFFF000000000000ull) != etag || fl == 0) continue;  // not published yet
+              excl += (long long)(w[i] & ((1ull << 46) - 1));
+              used = i + 1;
+              if (fl == RS_FLAG_PRE) fin = true;
+            }
+            jp -= used;
+            if (fin || jp < 0) break;
+            if (used == 0 && ++spins > spin_limit) {
+              gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX, tile);
+              break;
+            }
+          }
+          *(volatile unsigned long long*)(status + (size_t)tile * radix + d) =
+              etag | (RS_FLAG_PRE << 46) | (unsigned long long)(excl + tots[j]);
+        }
+        gpos[d] = (long long)gofs[d] + excl - (long long)bstart[d];
+      }
     }
   }
   __syncthreads();
-  // ---- write runs
-  const int cnt = (int)min((long long)RS_TILE, n - tbase);
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-    const unsigned long long k = s.k[i];
-    const unsigned d = (unsigned)((k >> shift) & mask);
-    const unsigned long long gp = s.gpos[d] + (unsigned long long)(i - (int)s.bstart[d]);
+
+  // ---- permute keys, then values, in place (all reads before a barrier, writes after)
+  unsigned pos[(IT + 1) / 2];
+  {
+    unsigned long long kk[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int idx = wbase + it * 32 + lane;
+      unsigned p = 0xFFFFu;
+      if (idx < cnt) {
+        kk[it] = sk[idx];
+        const unsigned d = rs_digit(kk[it], shift, mask);
+        const unsigned r = (it & 1) ? (rk[it >> 1] >> 16) : (rk[it >> 1] & 0xFFFFu);
+        p = bstart[d] + mywh[d] + r;
+      }
+      if (it & 1) pos[it >> 1] |= p << 16;
+      else pos[it >> 1] = p;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const unsigned p = (it & 1) ? (pos[it >> 1] >> 16) : (pos[it >> 1] & 0xFFFFu);
+      if (p != 0xFFFFu) sk[p] = kk[it];
+    }
+  }
+  {
+    unsigned vv[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int idx = wbase + it * 32 + lane;
+      if (idx < cnt) vv[it] = sv[idx];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const unsigned p = (it & 1) ? (pos[it >> 1] >> 16) : (pos[it >> 1] & 0xFFFFu);
+      if (p != 0xFFFFu) sv[p] = vv[it];
+    }
+  }
+  __syncthreads();
+  // ---- write runs: consecutive threads write consecutive slots of a digit's run
+  for (int i = tid; i < cnt; i += RS_THREADS) {
+    const unsigned long long k = sk[i];
+    const long long gp = gpos[rs_digit(k, shift, mask)] + i;
     kout[gp] = k;
-    vout[gp] = s.v[i];
+    vout[gp] = sv[i];
   }
 }
 
@@ -180,55 +391,152 @@ __global__ void k_rs_zero(unsigned* p, int n, long long* ctrs, int nc) {
   if (threadIdx.x < nc) ctrs[threadIdx.x] = 0;
 }
 
+// ---------------------------------------------------------------- host side
+namespace {
+
 struct RsState {
   unsigned* ghist = nullptr;
   unsigned long long* status = nullptr;
-  long long status_tiles = 0;
+  size_t status_words = 0;
   long long* ctrs = nullptr;
   unsigned long long epoch = 0;
-  bool attr = false;
 };
-static RsState g_rs;
+
+using PassFn = void (*)(const unsigned long long*, const unsigned*, unsigned long long*, unsigned*, long long,
+                        int, int, const unsigned*, unsigned long long*, unsigned long long, long long*, DStatus*,
+                        int, int);
+
+struct RsKernel {
+  int it;
+  PassFn fn;
+};
+const RsKernel kKernels[] = {{8, k_rs_pass<8>}, {12, k_rs_pass<12>}, {16, k_rs_pass<16>}, {20, k_rs_pass<20>}};
+
+const RsKernel* kernel_for(int it) {
+  for (const RsKernel& k : kKernels)
+    if (k.it == it) return &k;
+  return nullptr;
+}
+
+RsState* state_of(GbCtx& c) {
+  if (!c.rs) c.rs = new RsState();
+  return static_cast<RsState*>(c.rs);
+}
+
+void make_plan(int bits, int passes, RsPlan& p) {
+  p.np = passes;
+  int sh = 0, off = 0;
+  for (int i = 0; i < passes; ++i) {
+    const int w = bits / passes + (i < bits % passes ? 1 : 0);
+    p.shift[i] = sh;
+    p.bits[i] = w;
+    p.off[i] = off;
+    sh += w;
+    off += 1 << w;
+  }
+}
+
+// process-wide table of tuned configurations: (device, bits, log2 n) -> (passes, items per thread)
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
+
+int log2_bucket(long long n) {
+  int b = 0;
+  while ((1ll << (b + 1)) <= n) ++b;
+  return b;
+}
+
+}  // namespace
+
+void gb_radix_free(GbCtx& c) {
+  RsState* s = static_cast<RsState*>(c.rs);
+  if (!s) return;
+  cudaFree(s->ghist);
+  cudaFree(s->status);
+  cudaFree(s->ctrs);
+  delete s;
+  c.rs = nullptr;
+}
+
+// Default configuration for a sort of `bits` significant bits: the fewest
+// passes with digits of at most 8 bits, one more when that makes the count
+// even (it moves as many bytes as the final copy it saves, in narrower and
+// better-coalesced digit runs), 16 keys per thread.
+void gb_radix_default(int bits, int* passes, int* items) {
+  int p = (bits + 7) / 8;
+  if ((p & 1) && p + 1 <= bits) ++p;
+  *passes = std::max(1, p);
+  *items = 16;
+}
 
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
-                        unsigned long long* keys_tmp, unsigned* vals_tmp, int digit_bits) {
+                        unsigned long long* keys_tmp, unsigned* vals_tmp, int passes, int items) {
   if (n <= 1) return 0;
-  if (digit_bits < 1 || digit_bits > 8) digit_bits = 8;
-  int passes = (bits + digit_bits - 1) / digit_bits;
-  if (passes < 1) passes = 1;
-  if (passes > RS_MAXPASS) return -1;
-  const long long ntile = (n + RS_TILE - 1) / RS_TILE;
-  if (!g_rs.ghist) {
-    cudaMalloc(&g_rs.ghist, RS_MAXPASS * RS_RADIX * sizeof(unsigned));
-    cudaMalloc(&g_rs.ctrs, RS_MAXPASS * sizeof(long long));
+  if (bits < 1) bits = 1;
+  if (bits > 64) bits = 64;
+  if (passes <= 0 || items <= 0) {
+    int tp = 0, ti = 0;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto f = g_tuned.find(std::make_tuple(c.device, bits, log2_bucket(n)));
+      if (f != g_tuned.end()) {
+        tp = f->second.first;
+        ti = f->second.second;
+      }
+    }
+    if (!tp) gb_radix_default(bits, &tp, &ti);
+    if (passes <= 0) passes = tp;
+    if (items <= 0) items = ti;
   }
-  if (g_rs.status_tiles < ntile) {
-    if (g_rs.status) cudaFree(g_rs.status);
-    const long long want = ntile + 1024;
-    if (cudaMalloc(&g_rs.status, (size_t)want * RS_RADIX * 8) != cudaSuccess) return -2;
-    cudaMemsetAsync(g_rs.status, 0, (size_t)want * RS_RADIX * 8, c.stream);
-    g_rs.status_tiles = want;
+  if (passes > bits) passes = bits;
+  if (passes > RS_MAXPASS || (bits + passes - 1) / passes > 10) return -1;  // digits of 1..10 bits only
+  const RsKernel* K = kernel_for(items);
+  if (!K) return -1;
+  RsPlan plan;
+  make_plan(bits, passes, plan);
+  const int maxradix = 1 << plan.bits[0];
+  const int TILE = RS_THREADS * K->it;
+  const long long ntile = (n + TILE - 1) / TILE;
+  RsState* S = state_of(c);
+  if (!S->ghist) {
+    if (cudaMalloc(&S->ghist, RS_HIST_SLOTS * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&S->ctrs, RS_MAXPASS * sizeof(long long)) != cudaSuccess)
+      return -2;
   }
-  if (!g_rs.attr) {
-    cudaFuncSetAttribute(k_rs_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem));
-    g_rs.attr = true;
+  const size_t want = (size_t)(ntile + 1024) * maxradix;
+  if (S->status_words < want) {
+    if (S->status) cudaFree(S->status);
+    S->status = nullptr;
+    S->status_words = 0;
+    if (cudaMalloc(&S->status, want * 8) != cudaSuccess) return -2;
+    cudaMemsetAsync(S->status, 0, want * 8, c.stream);
+    S->status_words = want;
   }
-  k_rs_zero<<<1, 1024, 0, c.stream>>>(g_rs.ghist, RS_MAXPASS * RS_RADIX, g_rs.ctrs, RS_MAXPASS);
-  k_rs_hist<<<c.nsm * 4, RS_THREADS, 0, c.stream>>>(keys, n, passes, digit_bits, g_rs.ghist);
-  k_rs_hist_scan<<<passes, RS_RADIX, 0, c.stream>>>(g_rs.ghist, passes, 1 << digit_bits);
+  const size_t smem = rs_smem_bytes(K->it, maxradix);
+  cudaFuncSetAttribute((const void*)K->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute((const void*)K->fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  const bool al = !(((uintptr_t)keys | (uintptr_t)vals | (uintptr_t)keys_tmp | (uintptr_t)vals_tmp) & 15u);
+  k_rs_zero<<<1, 1024, 0, c.stream>>>(S->ghist, RS_HIST_SLOTS, S->ctrs, RS_MAXPASS);
+  if (!((uintptr_t)keys & 15u))
+    k_rs_hist<true><<<c.nsm * 4, 256, 0, c.stream>>>(keys, n, plan, S->ghist);
+  else
+    k_rs_hist<false><<<c.nsm * 4, 256, 0, c.stream>>>(keys, n, plan, S->ghist);
+  k_rs_hist_scan<<<passes, 1024, 0, c.stream>>>(S->ghist, plan);
+  c.launches += 3;
   unsigned long long* ka = keys;
   unsigned* va = vals;
   unsigned long long* kb = keys_tmp;
   unsigned* vb = vals_tmp;
   for (int p = 0; p < passes; ++p) {
-    g_rs.epoch = (g_rs.epoch + 1) & 0xFFFFull;
-    if (g_rs.epoch == 0) {
-      cudaMemsetAsync(g_rs.status, 0, (size_t)g_rs.status_tiles * RS_RADIX * 8, c.stream);
-      g_rs.epoch = 1;
+    S->epoch = (S->epoch + 1) & 0xFFFFull;
+    if (S->epoch == 0) {
+      cudaMemsetAsync(S->status, 0, S->status_words * 8, c.stream);
+      S->epoch = 1;
     }
-    k_rs_pass<<<(unsigned)ntile, RS_THREADS, sizeof(RsSmem), c.stream>>>(
-        ka, va, kb, vb, n, p * digit_bits, digit_bits, g_rs.ghist + p * RS_RADIX, g_rs.status,
-        g_rs.epoch, g_rs.ctrs + p, c.st, RS_SPIN_LIMIT);
+    K->fn<<<(unsigned)ntile, RS_THREADS, smem, c.stream>>>(ka, va, kb, vb, n, plan.shift[p], plan.bits[p],
+                                                          S->ghist + plan.off[p], S->status, S->epoch,
+                                                          S->ctrs + p, c.st, RS_SPIN_LIMIT, al ? 1 : 0);
+    ++c.launches;
     std::swap(ka, kb);
     std::swap(va, vb);
   }
@@ -239,25 +547,95 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
   return passes;
 }
 
+// Time each candidate (passes, keys per thread) on a copy of the caller's
+// keys and remember the fastest for this device, bit width and size class
+// (powers of two of n); later sorts in that class use it.
+int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals, long long n, int bits,
+                      int* best_passes, int* best_items, float* best_ms) {
+  if (n <= 1 || bits < 1 || bits > 64) return -1;
+  unsigned long long *k = nullptr, *kt = nullptr;
+  unsigned *v = nullptr, *vt = nullptr;
+  if (cudaMalloc(&k, (size_t)n * 8) != cudaSuccess || cudaMalloc(&kt, (size_t)n * 8) != cudaSuccess ||
+      cudaMalloc(&v, (size_t)n * 4) != cudaSuccess || cudaMalloc(&vt, (size_t)n * 4) != cudaSuccess) {
+    cudaFree(k);
+    cudaFree(kt);
+    cudaFree(v);
+    return -2;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int bp = 0, bi = 0;
+  float bms = 1e30f;
+  const int pmin = std::max(1, (bits + 9) / 10), pmax = std::min(bits, pmin + 3);
+  for (int p = pmin; p <= pmax; ++p) {
+    for (const RsKernel& K : kKernels) {
+      float tot = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {
+        cudaMemcpyAsync(k, keys, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream);
+        cudaMemcpyAsync(v, vals, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
+        cudaEventRecord(e0, c.stream);
+        const int r = gb_radix_sort_pairs(c, k, v, n, bits, kt, vt, p, K.it);
+        cudaEventRecord(e1, c.stream);
+        cudaEventSynchronize(e1);
+        if (r < 0) {
+          tot = 1e30f;
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep) tot += ms;  // the first run warms up
+      }
+      if (tot / 2 < bms) {
+        bms = tot / 2;
+        bp = p;
+        bi = K.it;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(k);
+  cudaFree(kt);
+  cudaFree(v);
+  cudaFree(vt);
+  if (!bp) return -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[std::make_tuple(c.device, bits, log2_bucket(n))] = {bp, bi};
+  }
+  if (best_passes) *best_passes = bp;
+  if (best_items) *best_items = bi;
+  if (best_ms) *best_ms = bms;
+  return 0;
+}
+
+void gb_radix_forget_tuning() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned.clear();
+}
+
 // Diagnostics for the bounded look-back: one CTA is handed tile 1 of a
 // two-tile pass, so it waits for a tile-0 status word that nothing ever
 // publishes.  After spin_limit polls it must flag GB_ERR_TIMEOUT and finish.
 __global__ void k_rs_set_counter(long long* c, long long v) { *c = v; }
 int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit) {
-  const long long n = 2 * RS_TILE;
+  constexpr int IT = 16, TILE = RS_THREADS * IT;
+  const long long n = 2 * TILE;
   unsigned long long *k = nullptr, *k2 = nullptr, *status = nullptr;
   unsigned *v = nullptr, *v2 = nullptr, *gofs = nullptr;
   long long* ctr = nullptr;
   cudaMalloc(&k, n * 8); cudaMalloc(&k2, n * 8); cudaMalloc(&v, n * 4); cudaMalloc(&v2, n * 4);
-  cudaMalloc(&status, 2 * RS_RADIX * 8); cudaMalloc(&gofs, RS_RADIX * 4); cudaMalloc(&ctr, 8);
+  cudaMalloc(&status, 2 * 256 * 8); cudaMalloc(&gofs, 256 * 4); cudaMalloc(&ctr, 8);
   cudaMemsetAsync(k, 0, n * 8, c.stream);
   cudaMemsetAsync(v, 0, n * 4, c.stream);
-  cudaMemsetAsync(status, 0, 2 * RS_RADIX * 8, c.stream);
-  cudaMemsetAsync(gofs, 0, RS_RADIX * 4, c.stream);
+  cudaMemsetAsync(status, 0, 2 * 256 * 8, c.stream);
+  cudaMemsetAsync(gofs, 0, 256 * 4, c.stream);
   k_rs_set_counter<<<1, 1, 0, c.stream>>>(ctr, 1);
-  cudaFuncSetAttribute(k_rs_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem));
-  k_rs_pass<<<1, RS_THREADS, sizeof(RsSmem), c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st,
-                                                        spin_limit);
+  const size_t smem = rs_smem_bytes(IT, 256);
+  cudaFuncSetAttribute((const void*)k_rs_pass<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_rs_pass<IT><<<1, RS_THREADS, smem, c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st, spin_limit,
+                                                   1);
   const cudaError_t e = cudaStreamSynchronize(c.stream);
   cudaFree(k); cudaFree(k2); cudaFree(v); cudaFree(v2); cudaFree(status); cudaFree(gofs); cudaFree(ctr);
   return e == cudaSuccess ? 0 : -1;

@@ -92,6 +92,9 @@ def lib():
         "gb_run_deck": (ctypes.c_int, [ctypes.c_char_p, P, u64, P]),
         "gb_debug_lookback_timeout": (ctypes.c_int, [P, ctypes.c_int]),
         "gb_radix_sort_device": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P]),
+        "gb_radix_sort_device_cfg": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int]),
+        "gb_radix_autotune": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P, P]),
+        "gb_radix_tuning_reset": (None, []),
         "gb_morton_keys_device": (ctypes.c_int, [P, P, i64, P, P]),
         "gb_serve_create": (ctypes.c_int, [ctypes.c_int, u64, ctypes.c_int, u64, pp]),
         "gb_serve_add_layer": (ctypes.c_int, [P, P, u64, P]),
@@ -275,6 +278,28 @@ class Context:
         b = _boxes(boxes).copy()
         self._chk(lib().gb_canonical_sort(self.h, b.ctypes.data, len(b)))
         return b
+
+    def radix_sort_device(self, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes=0, items=0):
+        """Sort n device (uint64 key, uint32 value) pairs in place by the low
+        `bits` key bits (asynchronous on the context stream).  passes/items 0:
+        the tuned or default configuration.  Returns the pass count."""
+        L = lib()
+        if passes or items:
+            r = L.gb_radix_sort_device_cfg(self.h, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes, items)
+        else:
+            r = L.gb_radix_sort_device(self.h, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp)
+        if r < 0:
+            self._chk(-r)
+        return r
+
+    def radix_autotune(self, keys_ptr, vals_ptr, n, bits):
+        """Time the built sort configurations on a copy of the pairs; the
+        fastest is used by later sorts of this size class.  Returns
+        (passes, items, ms)."""
+        p, it, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        self._chk(lib().gb_radix_autotune(self.h, keys_ptr, vals_ptr, n, bits, ctypes.byref(p), ctypes.byref(it),
+                                          ctypes.byref(ms)))
+        return p.value, it.value, ms.value
 
 
 # ---- the reference's own FFI, called exactly as the Fortran layer calls it
