@@ -177,7 +177,7 @@ int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys, unsigned* 
                          unsigned long long* d_keys_tmp, unsigned* d_vals_tmp);
 /* The same with an explicit configuration: `passes` passes splitting the
  * bits as evenly as possible (digits of 1..10 bits) and `items` keys per
- * thread (8, 12, 16 or 20; tile = 256 * items keys).  -GB_ERR_ARG when the
+ * thread (12, 16 or 20; tile = 256 * items keys).  -GB_ERR_ARG when the
  * configuration is not built.  No counterpart in the reference. */
 int gb_radix_sort_device_cfg(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n, int bits,
                              unsigned long long* d_keys_tmp, unsigned* d_vals_tmp, int passes, int items);

@@ -43,7 +43,7 @@ def rand_keys(n, bits, seed):
     return k, np.arange(n, dtype=np.uint32)
 
 
-@pytest.mark.parametrize("items", [8, 12, 16, 20])
+@pytest.mark.parametrize("items", [12, 16, 20])
 @pytest.mark.parametrize("bits,passes", [(8, 1), (20, 2), (20, 3), (40, 4), (40, 5), (40, 6), (52, 6), (52, 7),
                                          (52, 8), (64, 7), (64, 8)])
 def test_configs(ctx, items, bits, passes):
@@ -125,7 +125,7 @@ def test_autotune(ctx):
     torch.cuda.synchronize()
     try:
         p, it, ms = ctx.radix_autotune(kd.data_ptr(), vd.data_ptr(), n, bits)
-        assert 1 <= p <= bits and it in (8, 12, 16, 20) and ms > 0
+        assert 1 <= p <= bits and it in (12, 16, 20) and ms > 0
         # the inputs are untouched, and the default sort now runs the tuned configuration
         assert np.array_equal(kd.cpu().numpy().view(np.uint64), keys)
         k, v, pp = dev_sort(ctx, keys, vals, bits)

@@ -124,7 +124,7 @@ void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* pare
 // ---- radix sort (gb_radix.cu)
 // Sorts n (key, value) pairs by the low `bits` bits of the 64-bit keys.
 // tmp buffers must hold n entries each.  Stable.  passes / items (keys per
-// thread: 8, 12, 16 or 20) <= 0 take the tuned or default choice.  Returns
+// thread: 12, 16 or 20) <= 0 take the tuned or default choice.  Returns
 // the pass count, or < 0 when the configuration is not available.
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
                         unsigned long long* keys_tmp, unsigned* vals_tmp, int passes = 0, int items = 0);

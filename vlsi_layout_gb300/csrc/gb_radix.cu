@@ -8,7 +8,7 @@
 //  2. Each pass is one kernel: a CTA takes the next tile from an atomic
 //     counter (so tiles start in order) and pulls the tile's keys and values
 //     into shared memory with two bulk asynchronous copies completing on an
-//     mbarrier.  Warps rank the keys stably with warp match ranking, the CTA
+//     mbarrier.  Warps rank the keys stably with per-bit ballots, the CTA
 //     publishes its per-digit counts, and obtains the exclusive prefix of all
 //     earlier tiles by a decoupled look-back over a status array.  Keys and
 //     values are then permuted in place in shared memory by digit and
@@ -33,6 +33,7 @@
 #define RS_MAXPASS 16
 #define RS_HIST_SLOTS 8192
 #define RS_SPIN_LIMIT (1 << 22)
+#define RS_LBDEPTH 8  // predecessors a digit's thread polls per round trip
 #define KID_RADIX 40
 #define KID_RADIX_COPY 41
 
@@ -152,18 +153,210 @@ __device__ __forceinline__ bool rs_mbar_wait(unsigned a, int limit) {
 
 // ---------------------------------------------------------------- one pass
 // Shared memory of a pass with tile T = RS_THREADS * IT keys and radix R:
-//   keys T*8 | vals T*4 | wh[RS_WARPS][R] u16 | bstart[R] u32 | gpos[R] i64 | mbarrier, tile, scan scratch
+//   keys T*8 | vals T*4 | wh[RS_WARPS][R] u16 | bstart[R] u32 | gpos[R] u32 | mbarrier, tile, scan scratch
 __host__ __device__ constexpr size_t rs_smem_bytes(int it, int radix) {
-  return (size_t)RS_THREADS * it * 12 + (size_t)RS_WARPS * radix * 2 + (size_t)radix * 4 + (size_t)radix * 8 +
-         16 + 33 * 8;
+  return (size_t)RS_THREADS * it * 12 + (size_t)RS_WARPS * radix * 2 + (size_t)radix * 8 + 16 + 33 * 8;
 }
 
-__device__ __forceinline__ unsigned rs_digit(unsigned long long k, int shift, unsigned mask) {
-  return (unsigned)(k >> shift) & mask;
+// The digit [shift, shift + dbits) of a key, taken from its two 32-bit words
+// with one funnel shift (the word choice is uniform over the pass).
+struct RsDigit {
+  bool hiw;
+  int s;
+  unsigned mask;
+  __device__ RsDigit(int shift, unsigned m) : hiw(shift >= 32), s(shift & 31), mask(m) {}
+  __device__ __forceinline__ unsigned operator()(unsigned long long k) const {
+    const unsigned lo = (unsigned)k, hi = (unsigned)(k >> 32);
+    return __funnelshift_r(hiw ? hi : lo, hiw ? 0u : hi, s) & mask;
+  }
+};
+
+// The work on a tile resident in shared memory: rank, prefix, permutation,
+// look-back and write-out.  FULL: the tile holds TILE keys (no bounds tests).
+template <int IT, int MAXB, bool FULL>
+__device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, unsigned short* wh, unsigned* bstart,
+                                        unsigned* gpos, long long* tmp, const RsDigit& digit, int radix, int cnt,
+                                        long long tile, long long ntile, const unsigned* __restrict__ gofs,
+                                        unsigned long long* status, unsigned long long epoch, DStatus* st,
+                                        int spin_limit, unsigned long long* __restrict__ kout,
+                                        unsigned* __restrict__ vout) {
+  constexpr int TILE = RS_THREADS * IT;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  // ---- rank: warp w owns keys [w*32*IT, (w+1)*32*IT) in order.  Peers with
+  // the same digit are found by a warp match (odd items) or one ballot per
+  // digit bit (even items), so the match unit and the integer pipe share the
+  // work; the lowest peer adds the group to the warp's counter (two 16-bit counters share a 32-bit
+  // word; a count never exceeds 32*IT, so no carry crosses halves) and
+  // broadcasts the old value.  Keys stay in registers; ranks are packed two
+  // to a register.
+  const unsigned lt = (1u << lane) - 1u;
+  const int wbase = wid * 32 * IT;
+  unsigned short* mywh = wh + wid * radix;
+  unsigned* mywh32 = reinterpret_cast<unsigned*>(mywh);
+  unsigned long long kk[IT];
+  unsigned rd[(IT + 1) / 2];
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int idx = wbase + it * 32 + lane;
+    const bool ok = FULL || idx < cnt;
+    kk[it] = ok ? sk[idx] : 0ull;
+    const unsigned d = digit(kk[it]);
+    unsigned peers;
+    if (it & 1) {
+      // odd items: warp match (its own pipe), invalid lanes carry an out-of-range digit
+      peers = __match_any_sync(0xffffffffu, ok ? d : 0xFFFFFFFFu);
+    } else {
+      // even items: one ballot per digit bit (integer pipe)
+      peers = 0xffffffffu;
+      if (!FULL) {
+        const unsigned vm = __ballot_sync(0xffffffffu, ok);
+        peers = ok ? vm : ~vm;
+      }
+#pragma unroll
+      for (int b = 0; b < MAXB; ++b) {
+        const unsigned bit = (d >> b) & 1u;
+        const unsigned bb = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? bb : ~bb;
+      }
+    }
+    const int leader = __ffs(peers) - 1;
+    unsigned old = 0;
+    if (ok && lane == leader) old = atomicAdd(&mywh32[d >> 1], (unsigned)__popc(peers) << ((d & 1u) * 16));
+    old = __shfl_sync(0xffffffffu, old, leader);
+    const unsigned r = ((old >> ((d & 1u) * 16)) & 0xFFFFu) + __popc(peers & lt);
+    if (it & 1) rd[it >> 1] |= r << 16;
+    else rd[it >> 1] = r;
+  }
+  __syncthreads();
+
+  // ---- per digit: offsets over warps, tile total, aggregate published
+  // (loops over a thread's digits run to the compile-time bound 4 so the
+  // per-digit arrays stay in registers)
+  const int dpt = radix > RS_THREADS ? radix / RS_THREADS : 1;  // digits per thread (1..4)
+  const int d0 = tid * dpt;
+  const bool own = d0 < radix;
+  unsigned tots[4] = {0u, 0u, 0u, 0u};
+  long long tsum = 0;
+  const unsigned long long etag = (epoch & 0xFFFFull) << 48;
+  if (own) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < dpt) {
+        const int d = d0 + j;
+        unsigned tot = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) {
+          const unsigned c = wh[w * radix + d];
+          wh[w * radix + d] = (unsigned short)tot;
+          tot += c;
+        }
+        tots[j] = tot;
+        tsum += tot;
+        const unsigned long long flag = tile == 0 ? RS_FLAG_PRE : RS_FLAG_AGG;
+        *(volatile unsigned long long*)(status + (size_t)tile * radix + d) = etag | (flag << 46) | tot;
+      }
+    }
+  }
+  {
+    long long tt;
+    long long ex = gb_block_excl(tsum, tmp, &tt);
+    if (own) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (j < dpt) {
+          bstart[d0 + j] = (unsigned)ex;
+          ex += tots[j];
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- permute in place: every read of the key array happened before the
+  // last barrier, so keys go straight from registers to their slots; rd
+  // becomes the slot pair.  Values: all reads, a barrier, then the writes.
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    if (FULL || wbase + it * 32 + lane < cnt) {
+      const unsigned d = digit(kk[it]);
+      const unsigned r = (it & 1) ? (rd[it >> 1] >> 16) : (rd[it >> 1] & 0xFFFFu);
+      const unsigned p = bstart[d] + mywh[d] + r;
+      sk[p] = kk[it];
+      rd[it >> 1] = (it & 1) ? ((rd[it >> 1] & 0xFFFFu) | (p << 16)) : ((rd[it >> 1] & 0xFFFF0000u) | p);
+    }
+  }
+  {
+    unsigned vv[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int idx = wbase + it * 32 + lane;
+      if (FULL || idx < cnt) vv[it] = sv[idx];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IT; ++it)
+      if (FULL || wbase + it * 32 + lane < cnt) sv[(it & 1) ? (rd[it >> 1] >> 16) : (rd[it >> 1] & 0xFFFFu)] = vv[it];
+  }
+
+  // ---- decoupled look-back: the thread of digit d polls the status words of
+  // RS_LBDEPTH / (digits per thread) predecessors at once (a warp reads whole
+  // rows of the [tile][digit] array), sums aggregates up to the nearest
+  // inclusive prefix, and polls again from the first word not yet published.
+  if (own) {
+    constexpr int DEPTH = RS_LBDEPTH;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < dpt) {
+        const int d = d0 + j;
+        unsigned excl = 0;
+        if (tile > 0) {
+          long long jp = tile - 1;  // next predecessor to read
+          int spins = 0;
+          const int depth = DEPTH / dpt;
+          for (;;) {
+            unsigned long long w[DEPTH];
+#pragma unroll
+            for (int i = 0; i < DEPTH; ++i)
+              w[i] = (i < depth && jp - i >= 0) ? *(volatile unsigned long long*)(status + (size_t)(jp - i) * radix + d)
+                                               : 0ull;
+            int used = 0;
+            bool fin = false;
+#pragma unroll
+            for (int i = 0; i < DEPTH; ++i) {
+              if (fin || used < i || i >= depth || jp - i < 0) continue;
+              const unsigned long long fl = (w[i] >> 46) & 3ull;
+              if ((w[i] & 0xFFFF000000000000ull) != etag || fl == 0) continue;  // not published yet
+              excl += (unsigned)w[i];  // values are below 2^32
+              used = i + 1;
+              if (fl == RS_FLAG_PRE) fin = true;
+            }
+            jp -= used;
+            if (fin || jp < 0) break;
+            if (used == 0 && ++spins > spin_limit) {
+              gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX, tile);
+              break;
+            }
+          }
+          *(volatile unsigned long long*)(status + (size_t)tile * radix + d) =
+              etag | (RS_FLAG_PRE << 46) | (unsigned long long)(excl + tots[j]);
+        }
+        gpos[d] = gofs[d] + excl - bstart[d];  // modulo 2^32: slot + gpos < n < 2^32
+      }
+    }
+  }
+  __syncthreads();
+  // ---- write runs: consecutive threads write consecutive slots of a digit's run
+  for (int i = tid; i < (FULL ? TILE : cnt); i += RS_THREADS) {
+    const unsigned long long k = sk[i];
+    const unsigned gp = gpos[digit(k)] + (unsigned)i;
+    kout[gp] = k;
+    vout[gp] = sv[i];
+  }
 }
 
-template <int IT>
-__global__ void __launch_bounds__(RS_THREADS, IT <= 8 ? 5 : IT <= 16 ? 4 : 3)
+// IT keys per thread; digits of at most MAXB bits; n < 2^32.
+template <int IT, int MAXB>
+__global__ void __launch_bounds__(RS_THREADS, IT <= 12 ? 4 : 3)
 k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict__ vin,
           unsigned long long* __restrict__ kout, unsigned* __restrict__ vout, long long n, int shift, int dbits,
           const unsigned* __restrict__ gofs, unsigned long long* status, unsigned long long epoch,
@@ -171,12 +364,12 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
   constexpr int TILE = RS_THREADS * IT;
   extern __shared__ __align__(128) unsigned char smraw[];
   const int radix = 1 << dbits;
-  const unsigned mask = (unsigned)radix - 1u;
+  const RsDigit digit(shift, (unsigned)radix - 1u);
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(smraw);
   unsigned* sv = reinterpret_cast<unsigned*>(sk + TILE);
   unsigned short* wh = reinterpret_cast<unsigned short*>(sv + TILE);  // [RS_WARPS][radix]
   unsigned* bstart = reinterpret_cast<unsigned*>(wh + RS_WARPS * radix);
-  long long* gpos = reinterpret_cast<long long*>(bstart + radix);
+  unsigned* gpos = bstart + radix;
   unsigned long long* mbar = reinterpret_cast<unsigned long long*>(gpos + radix);
   long long* stile = reinterpret_cast<long long*>(mbar + 1);
   long long* tmp = stile + 1;  // [33]
@@ -223,167 +416,12 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
     __syncthreads();
   }
 
-  // ---- rank: warp w owns keys [w*32*IT, (w+1)*32*IT) in order.  Peers with
-  // the same digit are found by a warp match; the lowest peer adds the group
-  // to the warp's counter (two 16-bit counters share a 32-bit word; a count
-  // never exceeds 32*IT, so no carry crosses halves) and broadcasts the old
-  // value.
-  const unsigned lt = (1u << lane) - 1u;
-  const int wbase = wid * 32 * IT;
-  unsigned short* mywh = wh + wid * radix;
-  unsigned* mywh32 = reinterpret_cast<unsigned*>(mywh);
-  unsigned rk[(IT + 1) / 2];
-#pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const int idx = wbase + it * 32 + lane;
-    const bool ok = idx < cnt;
-    const unsigned d = ok ? rs_digit(sk[idx], shift, mask) : 0xFFFFu;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const int leader = __ffs(peers) - 1;
-    unsigned old = 0;
-    if (ok && lane == leader) old = atomicAdd(&mywh32[d >> 1], (unsigned)__popc(peers) << ((d & 1u) * 16));
-    old = __shfl_sync(0xffffffffu, old, leader);
-    const unsigned r = ((old >> ((d & 1u) * 16)) & 0xFFFFu) + __popc(peers & lt);
-    if (it & 1) rk[it >> 1] |= r << 16;
-    else rk[it >> 1] = r;
-  }
-  __syncthreads();
-
-  // ---- per digit: offsets over warps, tile total, aggregate published
-  // (loops over a thread's digits run to the compile-time bound 4 so the
-  // per-digit arrays stay in registers)
-  const int dpt = radix > RS_THREADS ? radix / RS_THREADS : 1;  // digits per thread (1..4)
-  const int d0 = tid * dpt;
-  const bool dig = d0 < radix;
-  unsigned tots[4] = {0u, 0u, 0u, 0u};
-  long long tsum = 0;
-  const unsigned long long etag = (epoch & 0xFFFFull) << 48;
-  if (dig) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j < dpt) {
-        const int d = d0 + j;
-        unsigned tot = 0;
-#pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) {
-          const unsigned c = wh[w * radix + d];
-          wh[w * radix + d] = (unsigned short)tot;
-          tot += c;
-        }
-        tots[j] = tot;
-        tsum += tot;
-        const unsigned long long flag = tile == 0 ? RS_FLAG_PRE : RS_FLAG_AGG;
-        *(volatile unsigned long long*)(status + (size_t)tile * radix + d) = etag | (flag << 46) | tot;
-      }
-    }
-  }
-  {
-    long long tt;
-    long long ex = gb_block_excl(tsum, tmp, &tt);
-    if (dig) {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (j < dpt) {
-          bstart[d0 + j] = (unsigned)ex;
-          ex += tots[j];
-        }
-      }
-    }
-  }
-  // ---- decoupled look-back: the thread of digit d polls the status words of
-  // DEPTH predecessors at once (a warp reads whole rows of the [tile][digit]
-  // array), sums aggregates up to the nearest inclusive prefix, and polls
-  // again from the first word that was not yet published.
-  if (dig) {
-    constexpr int DEPTH = 8;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (j < dpt) {
-        const int d = d0 + j;
-        long long excl = 0;
-        if (tile > 0) {
-          long long jp = tile - 1;  // next predecessor to read
-          int spins = 0;
-          const int depth = DEPTH / dpt;
-          for (;;) {
-            unsigned long long w[DEPTH];
-#pragma unroll
-            for (int i = 0; i < DEPTH; ++i)
-              w[i] = (i < depth && jp - i >= 0) ? *(volatile unsigned long long*)(status + (size_t)(jp - i) * radix + d)
-                                               : 0ull;
-            int used = 0;
-            bool fin = false;
-#pragma unroll
-            for (int i = 0; i < DEPTH; ++i) {
-              if (fin || used < i || i >= depth || jp - i < 0) continue;
-              const unsigned long long fl = (w[i] >> 46) & 3ull;
-              if ((w[i] & 0xFFFF000000000000ull) != etag || fl == 0) continue;  // not published yet
-              excl += (long long)(w[i] & ((1ull << 46) - 1));
-              used = i + 1;
-              if (fl == RS_FLAG_PRE) fin = true;
-            }
-            jp -= used;
-            if (fin || jp < 0) break;
-            if (used == 0 && ++spins > spin_limit) {
-              gb_set_error(st, GB_ERR_TIMEOUT, KID_RADIX, tile);
-              break;
-            }
-          }
-          *(volatile unsigned long long*)(status + (size_t)tile * radix + d) =
-              etag | (RS_FLAG_PRE << 46) | (unsigned long long)(excl + tots[j]);
-        }
-        gpos[d] = (long long)gofs[d] + excl - (long long)bstart[d];
-      }
-    }
-  }
-  __syncthreads();
-
-  // ---- permute keys, then values, in place (all reads before a barrier, writes after)
-  unsigned pos[(IT + 1) / 2];
-  {
-    unsigned long long kk[IT];
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-      const int idx = wbase + it * 32 + lane;
-      unsigned p = 0xFFFFu;
-      if (idx < cnt) {
-        kk[it] = sk[idx];
-        const unsigned d = rs_digit(kk[it], shift, mask);
-        const unsigned r = (it & 1) ? (rk[it >> 1] >> 16) : (rk[it >> 1] & 0xFFFFu);
-        p = bstart[d] + mywh[d] + r;
-      }
-      if (it & 1) pos[it >> 1] |= p << 16;
-      else pos[it >> 1] = p;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-      const unsigned p = (it & 1) ? (pos[it >> 1] >> 16) : (pos[it >> 1] & 0xFFFFu);
-      if (p != 0xFFFFu) sk[p] = kk[it];
-    }
-  }
-  {
-    unsigned vv[IT];
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-      const int idx = wbase + it * 32 + lane;
-      if (idx < cnt) vv[it] = sv[idx];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-      const unsigned p = (it & 1) ? (pos[it >> 1] >> 16) : (pos[it >> 1] & 0xFFFFu);
-      if (p != 0xFFFFu) sv[p] = vv[it];
-    }
-  }
-  __syncthreads();
-  // ---- write runs: consecutive threads write consecutive slots of a digit's run
-  for (int i = tid; i < cnt; i += RS_THREADS) {
-    const unsigned long long k = sk[i];
-    const long long gp = gpos[rs_digit(k, shift, mask)] + i;
-    kout[gp] = k;
-    vout[gp] = sv[i];
-  }
+  if (cnt == TILE)
+    rs_tile<IT, MAXB, true>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+                            spin_limit, kout, vout);
+  else
+    rs_tile<IT, MAXB, false>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+                             spin_limit, kout, vout);
 }
 
 __global__ void k_rs_zero(unsigned* p, int n, long long* ctrs, int nc) {
@@ -408,15 +446,21 @@ using PassFn = void (*)(const unsigned long long*, const unsigned*, unsigned lon
 
 struct RsKernel {
   int it;
-  PassFn fn;
+  PassFn fn[3];  // digits of at most 6, 8, 10 bits
 };
-const RsKernel kKernels[] = {{8, k_rs_pass<8>}, {12, k_rs_pass<12>}, {16, k_rs_pass<16>}, {20, k_rs_pass<20>}};
+const RsKernel kKernels[] = {
+    {12, {k_rs_pass<12, 6>, k_rs_pass<12, 8>, k_rs_pass<12, 10>}},
+    {16, {k_rs_pass<16, 6>, k_rs_pass<16, 8>, k_rs_pass<16, 10>}},
+    {20, {k_rs_pass<20, 6>, k_rs_pass<20, 8>, k_rs_pass<20, 10>}},
+};
 
 const RsKernel* kernel_for(int it) {
   for (const RsKernel& k : kKernels)
     if (k.it == it) return &k;
   return nullptr;
 }
+
+PassFn pass_fn(const RsKernel* K, int dbits) { return K->fn[dbits <= 6 ? 0 : dbits <= 8 ? 1 : 2]; }
 
 RsState* state_of(GbCtx& c) {
   if (!c.rs) c.rs = new RsState();
@@ -472,6 +516,7 @@ void gb_radix_default(int bits, int* passes, int* items) {
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
                         unsigned long long* keys_tmp, unsigned* vals_tmp, int passes, int items) {
   if (n <= 1) return 0;
+  if (n >= (1ll << 32)) return -1;  // slots and values are 32-bit
   if (bits < 1) bits = 1;
   if (bits > 64) bits = 64;
   if (passes <= 0 || items <= 0) {
@@ -513,8 +558,10 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     S->status_words = want;
   }
   const size_t smem = rs_smem_bytes(K->it, maxradix);
-  cudaFuncSetAttribute((const void*)K->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute((const void*)K->fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  for (int i = 0; i < 3; ++i) {
+    cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  }
   const bool al = !(((uintptr_t)keys | (uintptr_t)vals | (uintptr_t)keys_tmp | (uintptr_t)vals_tmp) & 15u);
   k_rs_zero<<<1, 1024, 0, c.stream>>>(S->ghist, RS_HIST_SLOTS, S->ctrs, RS_MAXPASS);
   if (!((uintptr_t)keys & 15u))
@@ -533,7 +580,8 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
       cudaMemsetAsync(S->status, 0, S->status_words * 8, c.stream);
       S->epoch = 1;
     }
-    K->fn<<<(unsigned)ntile, RS_THREADS, smem, c.stream>>>(ka, va, kb, vb, n, plan.shift[p], plan.bits[p],
+    pass_fn(K, plan.bits[p])<<<(unsigned)ntile, RS_THREADS, smem, c.stream>>>(ka, va, kb, vb, n, plan.shift[p],
+                                                                              plan.bits[p],
                                                           S->ghist + plan.off[p], S->status, S->epoch,
                                                           S->ctrs + p, c.st, RS_SPIN_LIMIT, al ? 1 : 0);
     ++c.launches;
@@ -633,8 +681,8 @@ int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit) {
   cudaMemsetAsync(gofs, 0, 256 * 4, c.stream);
   k_rs_set_counter<<<1, 1, 0, c.stream>>>(ctr, 1);
   const size_t smem = rs_smem_bytes(IT, 256);
-  cudaFuncSetAttribute((const void*)k_rs_pass<IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_rs_pass<IT><<<1, RS_THREADS, smem, c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st, spin_limit,
+  cudaFuncSetAttribute((const void*)k_rs_pass<IT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_rs_pass<IT, 8><<<1, RS_THREADS, smem, c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st, spin_limit,
                                                    1);
   const cudaError_t e = cudaStreamSynchronize(c.stream);
   cudaFree(k); cudaFree(k2); cudaFree(v); cudaFree(v2); cudaFree(status); cudaFree(gofs); cudaFree(ctr);
