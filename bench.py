@@ -240,9 +240,9 @@ def sort_leg(n=200_000_000, steps=5, seed=5, tune=True):
         L.gb_radix_tuning_reset()
         timed("default")
         if tune:
-            p, items, tms = ctx.radix_autotune(k0.data_ptr(), v0.data_ptr(), n, bits)
+            p, tile, tms = ctx.radix_autotune(k0.data_ptr(), v0.data_ptr(), n, bits)
             timed("tuned")
-            out["tuned"]["items_per_thread"] = items
+            out["tuned"]["tile_keys"] = tile
             L.gb_radix_tuning_reset()
     best = min((out[k] for k in ("default", "tuned") if k in out), key=lambda r: r["ms"])
     out.update({k: best[k] for k in ("passes", "ms", "keys_per_s", "gb_s", "frac_of_peak", "sorted")})

@@ -169,25 +169,26 @@ int gb_morton_sort(gb_context* ctx, c_box* boxes, long long n, int sort_boxes,
  * in d_keys / d_vals.  The pass count and keys per thread come from the
  * autotuner's table when it holds this device, bit width and size class,
  * else from the default (digits of at most 8 bits, an even pass count when
- * that costs no extra pass of bytes, 16 keys per thread).  Returns the number
+ * that costs no extra pass of bytes, tiles of 5120 keys).  n < 2^32.  Returns the number
  * of passes (>= 0) or minus a GB_ERR_* status.  Asynchronous on the context stream.
  * Replaces the Thrust radix sorts of gpu_morton.cu:149-187 and
  * event_sorter.cu:64-81 on device-resident data. */
 int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n, int bits,
                          unsigned long long* d_keys_tmp, unsigned* d_vals_tmp);
 /* The same with an explicit configuration: `passes` passes splitting the
- * bits as evenly as possible (digits of 1..10 bits) and `items` keys per
- * thread (12, 16 or 20; tile = 256 * items keys).  -GB_ERR_ARG when the
- * configuration is not built.  No counterpart in the reference. */
+ * bits as evenly as possible (digits of 1..10 bits) and CTA tiles of `tile`
+ * keys (3072, 4096, 5120 on 256 threads; 6144, 8192 on 512 threads).
+ * -GB_ERR_ARG when the configuration is not built.  No counterpart in the
+ * reference. */
 int gb_radix_sort_device_cfg(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n, int bits,
-                             unsigned long long* d_keys_tmp, unsigned* d_vals_tmp, int passes, int items);
-/* Autotuner: times every built (passes, items) pair near the fewest passes on
+                             unsigned long long* d_keys_tmp, unsigned* d_vals_tmp, int passes, int tile);
+/* Autotuner: times every built (passes, tile) pair near the fewest passes on
  * a device copy of the given pairs (inputs untouched; needs 2 x 12 n bytes of
  * device memory), keeps the fastest in a process-wide table keyed by device,
  * bit width and power-of-two size class, and returns it.  Synchronous.  No
  * counterpart in the reference. */
 int gb_radix_autotune(gb_context* ctx, const unsigned long long* d_keys, const unsigned* d_vals, long long n,
-                      int bits, int* passes, int* items, float* ms);
+                      int bits, int* passes, int* tile, float* ms);
 /* Clear the autotuner's table (later sorts use the default again). */
 void gb_radix_tuning_reset(void);
 /* Morton keys of device boxes (gpu_morton.cu:113-144) and the identity

@@ -1,6 +1,6 @@
 """Device radix sort (the Morton / event-key sort of gpu_morton.cu:149-187 and
 event_sorter.cu:64-81) against a stable numpy sort of the same keys: every
-built configuration (pass count x keys per thread), ragged sizes around the
+built configuration (pass count x tile size), ragged sizes around the
 tile edges, unaligned buffers (plain-load path), skewed digit distributions,
 Morton keys of real box shapes, and the autotuner."""
 import numpy as np
@@ -17,7 +17,7 @@ def expect(keys, vals, bits):
     return keys[o], vals[o]
 
 
-def dev_sort(ctx, keys, vals, bits, passes=0, items=0, offset=0):
+def dev_sort(ctx, keys, vals, bits, passes=0, tile=0, offset=0):
     """Sort on the device; offset > 0 shifts the buffers by that many elements
     so they are not 16-byte aligned."""
     n = len(keys)
@@ -30,7 +30,7 @@ def dev_sort(ctx, keys, vals, bits, passes=0, items=0, offset=0):
     torch.cuda.synchronize()
     k, v = kb[offset:], vb[offset:]
     p = ctx.radix_sort_device(k.data_ptr(), v.data_ptr(), n, bits, kt[offset:].data_ptr(), vt[offset:].data_ptr(),
-                              passes, items)
+                              passes, tile)
     ctx.sync()
     return k.cpu().numpy().view(np.uint64), v.cpu().numpy().view(np.uint32), p
 
@@ -43,12 +43,12 @@ def rand_keys(n, bits, seed):
     return k, np.arange(n, dtype=np.uint32)
 
 
-@pytest.mark.parametrize("items", [12, 16, 20])
+@pytest.mark.parametrize("tile", [3072, 4096, 5120, 6144, 8192])
 @pytest.mark.parametrize("bits,passes", [(8, 1), (20, 2), (20, 3), (40, 4), (40, 5), (40, 6), (52, 6), (52, 7),
                                          (52, 8), (64, 7), (64, 8)])
-def test_configs(ctx, items, bits, passes):
+def test_configs(ctx, tile, bits, passes):
     keys, vals = rand_keys(300_007, bits, seed=bits * 31 + passes)
-    k, v, p = dev_sort(ctx, keys, vals, bits, passes, items)
+    k, v, p = dev_sort(ctx, keys, vals, bits, passes, tile)
     ek, ev = expect(keys, vals, bits)
     assert p == passes
     assert np.array_equal(k, ek) and np.array_equal(v, ev)
@@ -111,9 +111,9 @@ def test_bad_configuration(ctx):
     from vlsi_layout_gb300 import engine
     keys, vals = rand_keys(1000, 40, seed=1)
     with pytest.raises(engine.GBError):
-        dev_sort(ctx, keys, vals, 40, passes=2, items=16)  # 20-bit digits are not built
+        dev_sort(ctx, keys, vals, 40, passes=2, tile=4096)  # 20-bit digits are not built
     with pytest.raises(engine.GBError):
-        dev_sort(ctx, keys, vals, 40, passes=5, items=10)  # 10 keys per thread is not built
+        dev_sort(ctx, keys, vals, 40, passes=5, tile=1000)  # no kernel has 1000-key tiles
 
 
 def test_autotune(ctx):
@@ -125,7 +125,7 @@ def test_autotune(ctx):
     torch.cuda.synchronize()
     try:
         p, it, ms = ctx.radix_autotune(kd.data_ptr(), vd.data_ptr(), n, bits)
-        assert 1 <= p <= bits and it in (12, 16, 20) and ms > 0
+        assert 1 <= p <= bits and it in (3072, 4096, 5120, 6144, 8192) and ms > 0
         # the inputs are untouched, and the default sort now runs the tuned configuration
         assert np.array_equal(kd.cpu().numpy().view(np.uint64), keys)
         k, v, pp = dev_sort(ctx, keys, vals, bits)

@@ -849,18 +849,18 @@ extern "C" int gb_radix_sort_device(gb_context* ctx, unsigned long long* d_keys,
 
 extern "C" int gb_radix_sort_device_cfg(gb_context* ctx, unsigned long long* d_keys, unsigned* d_vals, long long n,
                                         int bits, unsigned long long* d_keys_tmp, unsigned* d_vals_tmp, int passes,
-                                        int items) {
+                                        int tile) {
   if (!ctx || n < 0 || bits < 1 || bits > 64 || (n > 1 && (!d_keys || !d_vals || !d_keys_tmp || !d_vals_tmp)))
     return -GB_ERR_ARG;
-  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp, passes, items);
+  const int p = gb_radix_sort_pairs(ctx->c, d_keys, d_vals, n, bits, d_keys_tmp, d_vals_tmp, passes, tile);
   if (p == -2) return -set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in radix sort");
   return p < 0 ? -set_err(ctx, GB_ERR_ARG, "radix sort configuration not available") : p;
 }
 
 extern "C" int gb_radix_autotune(gb_context* ctx, const unsigned long long* d_keys, const unsigned* d_vals,
-                                 long long n, int bits, int* passes, int* items, float* ms) {
+                                 long long n, int bits, int* passes, int* tile, float* ms) {
   if (!ctx || n < 2 || bits < 1 || bits > 64 || !d_keys || !d_vals) return GB_ERR_ARG;
-  const int r = gb_radix_tune(ctx->c, d_keys, d_vals, n, bits, passes, items, ms);
+  const int r = gb_radix_tune(ctx->c, d_keys, d_vals, n, bits, passes, tile, ms);
   if (r == -2) return set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in radix autotune");
   if (r < 0) return set_err(ctx, GB_ERR_INTERNAL, "radix autotune found no configuration");
   return gb_sync(ctx, nullptr);

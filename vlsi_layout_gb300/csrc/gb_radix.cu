@@ -28,8 +28,6 @@
 #include "gb_internal.h"
 #include "gb_scan.cuh"
 
-#define RS_THREADS 256
-#define RS_WARPS (RS_THREADS / 32)
 #define RS_MAXPASS 16
 #define RS_HIST_SLOTS 8192
 #define RS_SPIN_LIMIT (1 << 22)
@@ -152,10 +150,10 @@ __device__ __forceinline__ bool rs_mbar_wait(unsigned a, int limit) {
 }
 
 // ---------------------------------------------------------------- one pass
-// Shared memory of a pass with tile T = RS_THREADS * IT keys and radix R:
-//   keys T*8 | vals T*4 | wh[RS_WARPS][R] u16 | bstart[R] u32 | gpos[R] u32 | mbarrier, tile, scan scratch
-__host__ __device__ constexpr size_t rs_smem_bytes(int it, int radix) {
-  return (size_t)RS_THREADS * it * 12 + (size_t)RS_WARPS * radix * 2 + (size_t)radix * 8 + 16 + 33 * 8;
+// Shared memory of a pass with NT threads, tile T = NT * IT keys and radix R:
+//   keys T*8 | vals T*4 | wh[NT/32][R] u16 | bstart[R] u32 | gpos[R] u32 | mbarrier, tile, scan scratch
+__host__ __device__ constexpr size_t rs_smem_bytes(int nt, int it, int radix) {
+  return (size_t)nt * it * 12 + (size_t)(nt / 32) * radix * 2 + (size_t)radix * 8 + 16 + 33 * 8;
 }
 
 // The digit [shift, shift + dbits) of a key, taken from its two 32-bit words
@@ -173,19 +171,20 @@ struct RsDigit {
 
 // The work on a tile resident in shared memory: rank, prefix, permutation,
 // look-back and write-out.  FULL: the tile holds TILE keys (no bounds tests).
-template <int IT, int MAXB, bool FULL>
+template <int NT, int IT, int MAXB, bool FULL>
 __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, unsigned short* wh, unsigned* bstart,
                                         unsigned* gpos, long long* tmp, const RsDigit& digit, int radix, int cnt,
                                         long long tile, long long ntile, const unsigned* __restrict__ gofs,
                                         unsigned long long* status, unsigned long long epoch, DStatus* st,
                                         int spin_limit, unsigned long long* __restrict__ kout,
                                         unsigned* __restrict__ vout) {
-  constexpr int TILE = RS_THREADS * IT;
+  constexpr int TILE = NT * IT;
+  constexpr int NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   // ---- rank: warp w owns keys [w*32*IT, (w+1)*32*IT) in order.  Peers with
-  // the same digit are found by a warp match (odd items) or one ballot per
-  // digit bit (even items), so the match unit and the integer pipe share the
-  // work; the lowest peer adds the group to the warp's counter (two 16-bit counters share a 32-bit
+  // the same digit are found by a warp match (every third item) or one
+  // ballot per digit bit (the others), so the match unit and the integer pipe
+  // share the work; the lowest peer adds the group to the warp's counter (two 16-bit counters share a 32-bit
   // word; a count never exceeds 32*IT, so no carry crosses halves) and
   // broadcasts the old value.  Keys stay in registers; ranks are packed two
   // to a register.
@@ -202,11 +201,11 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
     kk[it] = ok ? sk[idx] : 0ull;
     const unsigned d = digit(kk[it]);
     unsigned peers;
-    if (it & 1) {
-      // odd items: warp match (its own pipe), invalid lanes carry an out-of-range digit
+    if (it % 3 == 1) {
+      // every third item: warp match (its own pipe), invalid lanes carry an out-of-range digit
       peers = __match_any_sync(0xffffffffu, ok ? d : 0xFFFFFFFFu);
     } else {
-      // even items: one ballot per digit bit (integer pipe)
+      // the others: one ballot per digit bit (integer pipe)
       peers = 0xffffffffu;
       if (!FULL) {
         const unsigned vm = __ballot_sync(0xffffffffu, ok);
@@ -229,10 +228,11 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
   }
   __syncthreads();
 
-  // ---- per digit: offsets over warps, tile total, aggregate published
-  // (loops over a thread's digits run to the compile-time bound 4 so the
-  // per-digit arrays stay in registers)
-  const int dpt = radix > RS_THREADS ? radix / RS_THREADS : 1;  // digits per thread (1..4)
+  // ---- per digit: tile total (published as the tile's aggregate), the
+  // tile's bucket start, and each warp's first slot of the digit, folded
+  // into the warp counters (loops over a thread's digits run to the
+  // compile-time bound 4 so the per-digit arrays stay in registers)
+  const int dpt = radix > NT ? radix / NT : 1;  // digits per thread (1..4)
   const int d0 = tid * dpt;
   const bool own = d0 < radix;
   unsigned tots[4] = {0u, 0u, 0u, 0u};
@@ -245,13 +245,10 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
         const int d = d0 + j;
         unsigned tot = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) {
-          const unsigned c = wh[w * radix + d];
-          wh[w * radix + d] = (unsigned short)tot;
-          tot += c;
-        }
+        for (int w = 0; w < NW; ++w) tot += wh[w * radix + d];
         tots[j] = tot;
         tsum += tot;
+        gpos[d] = tot;  // kept for the look-back, which replaces it
         const unsigned long long flag = tile == 0 ? RS_FLAG_PRE : RS_FLAG_AGG;
         *(volatile unsigned long long*)(status + (size_t)tile * radix + d) = etag | (flag << 46) | tot;
       }
@@ -264,7 +261,15 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (j < dpt) {
-          bstart[d0 + j] = (unsigned)ex;
+          const int d = d0 + j;
+          bstart[d] = (unsigned)ex;
+          unsigned run = (unsigned)ex;
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            const unsigned c = wh[w * radix + d];
+            wh[w * radix + d] = (unsigned short)run;
+            run += c;
+          }
           ex += tots[j];
         }
       }
@@ -280,7 +285,7 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
     if (FULL || wbase + it * 32 + lane < cnt) {
       const unsigned d = digit(kk[it]);
       const unsigned r = (it & 1) ? (rd[it >> 1] >> 16) : (rd[it >> 1] & 0xFFFFu);
-      const unsigned p = bstart[d] + mywh[d] + r;
+      const unsigned p = mywh[d] + r;
       sk[p] = kk[it];
       rd[it >> 1] = (it & 1) ? ((rd[it >> 1] & 0xFFFFu) | (p << 16)) : ((rd[it >> 1] & 0xFFFF0000u) | p);
     }
@@ -346,7 +351,7 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
   }
   __syncthreads();
   // ---- write runs: consecutive threads write consecutive slots of a digit's run
-  for (int i = tid; i < (FULL ? TILE : cnt); i += RS_THREADS) {
+  for (int i = tid; i < (FULL ? TILE : cnt); i += NT) {
     const unsigned long long k = sk[i];
     const unsigned gp = gpos[digit(k)] + (unsigned)i;
     kout[gp] = k;
@@ -354,26 +359,27 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
   }
 }
 
-// IT keys per thread; digits of at most MAXB bits; n < 2^32.
-template <int IT, int MAXB>
-__global__ void __launch_bounds__(RS_THREADS, IT <= 12 ? 4 : 3)
+// NT threads, IT keys per thread; digits of at most MAXB bits; n < 2^32.
+template <int NT, int IT, int MAXB>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : (IT <= 12 ? 4 : 3))
 k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict__ vin,
           unsigned long long* __restrict__ kout, unsigned* __restrict__ vout, long long n, int shift, int dbits,
           const unsigned* __restrict__ gofs, unsigned long long* status, unsigned long long epoch,
           long long* counter, DStatus* st, int spin_limit, int bulk) {
-  constexpr int TILE = RS_THREADS * IT;
+  constexpr int TILE = NT * IT;
+  constexpr int NW = NT / 32;
   extern __shared__ __align__(128) unsigned char smraw[];
   const int radix = 1 << dbits;
   const RsDigit digit(shift, (unsigned)radix - 1u);
   unsigned long long* sk = reinterpret_cast<unsigned long long*>(smraw);
   unsigned* sv = reinterpret_cast<unsigned*>(sk + TILE);
-  unsigned short* wh = reinterpret_cast<unsigned short*>(sv + TILE);  // [RS_WARPS][radix]
-  unsigned* bstart = reinterpret_cast<unsigned*>(wh + RS_WARPS * radix);
+  unsigned short* wh = reinterpret_cast<unsigned short*>(sv + TILE);  // [NW][radix]
+  unsigned* bstart = reinterpret_cast<unsigned*>(wh + NW * radix);
   unsigned* gpos = bstart + radix;
   unsigned long long* mbar = reinterpret_cast<unsigned long long*>(gpos + radix);
   long long* stile = reinterpret_cast<long long*>(mbar + 1);
   long long* tmp = stile + 1;  // [33]
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int tid = threadIdx.x;
   const long long ntile = (n + TILE - 1) / TILE;
   const unsigned mb = rs_smem(mbar);
 
@@ -391,14 +397,14 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
       }
     }
   }
-  for (int i = tid; i < RS_WARPS * radix / 2; i += RS_THREADS) reinterpret_cast<unsigned*>(wh)[i] = 0u;
+  for (int i = tid; i < NW * radix / 2; i += NT) reinterpret_cast<unsigned*>(wh)[i] = 0u;
   __syncthreads();
   const long long tile = *stile;
   if (tile >= ntile) return;
   const long long tb = tile * TILE;
   const int cnt = (int)min((long long)TILE, n - tb);
   if (bulk) {
-    for (int i = (cnt & ~3) + tid; i < cnt; i += RS_THREADS) {
+    for (int i = (cnt & ~3) + tid; i < cnt; i += NT) {
       sk[i] = kin[tb + i];
       sv[i] = vin[tb + i];
     }
@@ -409,7 +415,7 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
       return;
     }
   } else {
-    for (int i = tid; i < cnt; i += RS_THREADS) {
+    for (int i = tid; i < cnt; i += NT) {
       sk[i] = kin[tb + i];
       sv[i] = vin[tb + i];
     }
@@ -417,10 +423,10 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
   }
 
   if (cnt == TILE)
-    rs_tile<IT, MAXB, true>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+    rs_tile<NT, IT, MAXB, true>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
                             spin_limit, kout, vout);
   else
-    rs_tile<IT, MAXB, false>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+    rs_tile<NT, IT, MAXB, false>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
                              spin_limit, kout, vout);
 }
 
@@ -445,22 +451,26 @@ using PassFn = void (*)(const unsigned long long*, const unsigned*, unsigned lon
                         int, int);
 
 struct RsKernel {
-  int it;
-  PassFn fn[3];  // digits of at most 6, 8, 10 bits
+  int nt, it;
+  PassFn fn[4];  // digits of at most 6, 7, 8, 10 bits
+  int tile() const { return nt * it; }
 };
 const RsKernel kKernels[] = {
-    {12, {k_rs_pass<12, 6>, k_rs_pass<12, 8>, k_rs_pass<12, 10>}},
-    {16, {k_rs_pass<16, 6>, k_rs_pass<16, 8>, k_rs_pass<16, 10>}},
-    {20, {k_rs_pass<20, 6>, k_rs_pass<20, 8>, k_rs_pass<20, 10>}},
+    {256, 12, {k_rs_pass<256, 12, 6>, k_rs_pass<256, 12, 7>, k_rs_pass<256, 12, 8>, k_rs_pass<256, 12, 10>}},
+    {256, 16, {k_rs_pass<256, 16, 6>, k_rs_pass<256, 16, 7>, k_rs_pass<256, 16, 8>, k_rs_pass<256, 16, 10>}},
+    {256, 20, {k_rs_pass<256, 20, 6>, k_rs_pass<256, 20, 7>, k_rs_pass<256, 20, 8>, k_rs_pass<256, 20, 10>}},
+    {512, 12, {k_rs_pass<512, 12, 6>, k_rs_pass<512, 12, 7>, k_rs_pass<512, 12, 8>, k_rs_pass<512, 12, 10>}},
+    {512, 16, {k_rs_pass<512, 16, 6>, k_rs_pass<512, 16, 7>, k_rs_pass<512, 16, 8>, k_rs_pass<512, 16, 10>}},
 };
 
-const RsKernel* kernel_for(int it) {
+// the kernel whose tile holds `tile` keys
+const RsKernel* kernel_for(int tile) {
   for (const RsKernel& k : kKernels)
-    if (k.it == it) return &k;
+    if (k.tile() == tile) return &k;
   return nullptr;
 }
 
-PassFn pass_fn(const RsKernel* K, int dbits) { return K->fn[dbits <= 6 ? 0 : dbits <= 8 ? 1 : 2]; }
+PassFn pass_fn(const RsKernel* K, int dbits) { return K->fn[dbits <= 6 ? 0 : dbits == 7 ? 1 : dbits == 8 ? 2 : 3]; }
 
 RsState* state_of(GbCtx& c) {
   if (!c.rs) c.rs = new RsState();
@@ -480,7 +490,7 @@ void make_plan(int bits, int passes, RsPlan& p) {
   }
 }
 
-// process-wide table of tuned configurations: (device, bits, log2 n) -> (passes, items per thread)
+// process-wide table of tuned configurations: (device, bits, log2 n) -> (passes, tile keys)
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
 
@@ -505,21 +515,21 @@ void gb_radix_free(GbCtx& c) {
 // Default configuration for a sort of `bits` significant bits: the fewest
 // passes with digits of at most 8 bits, one more when that makes the count
 // even (it moves as many bytes as the final copy it saves, in narrower and
-// better-coalesced digit runs), 16 keys per thread.
-void gb_radix_default(int bits, int* passes, int* items) {
+// better-coalesced digit runs), tiles of 8192 keys.
+void gb_radix_default(int bits, int* passes, int* tile) {
   int p = (bits + 7) / 8;
   if ((p & 1) && p + 1 <= bits) ++p;
   *passes = std::max(1, p);
-  *items = 16;
+  *tile = 8192;
 }
 
 int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long long n, int bits,
-                        unsigned long long* keys_tmp, unsigned* vals_tmp, int passes, int items) {
+                        unsigned long long* keys_tmp, unsigned* vals_tmp, int passes, int tile) {
   if (n <= 1) return 0;
   if (n >= (1ll << 32)) return -1;  // slots and values are 32-bit
   if (bits < 1) bits = 1;
   if (bits > 64) bits = 64;
-  if (passes <= 0 || items <= 0) {
+  if (passes <= 0 || tile <= 0) {
     int tp = 0, ti = 0;
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -531,16 +541,16 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     }
     if (!tp) gb_radix_default(bits, &tp, &ti);
     if (passes <= 0) passes = tp;
-    if (items <= 0) items = ti;
+    if (tile <= 0) tile = ti;
   }
   if (passes > bits) passes = bits;
   if (passes > RS_MAXPASS || (bits + passes - 1) / passes > 10) return -1;  // digits of 1..10 bits only
-  const RsKernel* K = kernel_for(items);
+  const RsKernel* K = kernel_for(tile);
   if (!K) return -1;
   RsPlan plan;
   make_plan(bits, passes, plan);
   const int maxradix = 1 << plan.bits[0];
-  const int TILE = RS_THREADS * K->it;
+  const int TILE = K->tile();
   const long long ntile = (n + TILE - 1) / TILE;
   RsState* S = state_of(c);
   if (!S->ghist) {
@@ -557,8 +567,8 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     cudaMemsetAsync(S->status, 0, want * 8, c.stream);
     S->status_words = want;
   }
-  const size_t smem = rs_smem_bytes(K->it, maxradix);
-  for (int i = 0; i < 3; ++i) {
+  const size_t smem = rs_smem_bytes(K->nt, K->it, maxradix);
+  for (int i = 0; i < 4; ++i) {
     cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   }
@@ -580,7 +590,7 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
       cudaMemsetAsync(S->status, 0, S->status_words * 8, c.stream);
       S->epoch = 1;
     }
-    pass_fn(K, plan.bits[p])<<<(unsigned)ntile, RS_THREADS, smem, c.stream>>>(ka, va, kb, vb, n, plan.shift[p],
+    pass_fn(K, plan.bits[p])<<<(unsigned)ntile, K->nt, smem, c.stream>>>(ka, va, kb, vb, n, plan.shift[p],
                                                                               plan.bits[p],
                                                           S->ghist + plan.off[p], S->status, S->epoch,
                                                           S->ctrs + p, c.st, RS_SPIN_LIMIT, al ? 1 : 0);
@@ -595,11 +605,11 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
   return passes;
 }
 
-// Time each candidate (passes, keys per thread) on a copy of the caller's
+// Time each candidate (passes, tile keys) on a copy of the caller's
 // keys and remember the fastest for this device, bit width and size class
 // (powers of two of n); later sorts in that class use it.
 int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals, long long n, int bits,
-                      int* best_passes, int* best_items, float* best_ms) {
+                      int* best_passes, int* best_tile, float* best_ms) {
   if (n <= 1 || bits < 1 || bits > 64) return -1;
   unsigned long long *k = nullptr, *kt = nullptr;
   unsigned *v = nullptr, *vt = nullptr;
@@ -623,7 +633,7 @@ int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals
         cudaMemcpyAsync(k, keys, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream);
         cudaMemcpyAsync(v, vals, (size_t)n * 4, cudaMemcpyDeviceToDevice, c.stream);
         cudaEventRecord(e0, c.stream);
-        const int r = gb_radix_sort_pairs(c, k, v, n, bits, kt, vt, p, K.it);
+        const int r = gb_radix_sort_pairs(c, k, v, n, bits, kt, vt, p, K.tile());
         cudaEventRecord(e1, c.stream);
         cudaEventSynchronize(e1);
         if (r < 0) {
@@ -637,7 +647,7 @@ int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals
       if (tot / 2 < bms) {
         bms = tot / 2;
         bp = p;
-        bi = K.it;
+        bi = K.tile();
       }
     }
   }
@@ -653,7 +663,7 @@ int gb_radix_tune(GbCtx& c, const unsigned long long* keys, const unsigned* vals
     g_tuned[std::make_tuple(c.device, bits, log2_bucket(n))] = {bp, bi};
   }
   if (best_passes) *best_passes = bp;
-  if (best_items) *best_items = bi;
+  if (best_tile) *best_tile = bi;
   if (best_ms) *best_ms = bms;
   return 0;
 }
@@ -668,7 +678,7 @@ void gb_radix_forget_tuning() {
 // publishes.  After spin_limit polls it must flag GB_ERR_TIMEOUT and finish.
 __global__ void k_rs_set_counter(long long* c, long long v) { *c = v; }
 int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit) {
-  constexpr int IT = 16, TILE = RS_THREADS * IT;
+  constexpr int NT = 256, IT = 16, TILE = NT * IT;
   const long long n = 2 * TILE;
   unsigned long long *k = nullptr, *k2 = nullptr, *status = nullptr;
   unsigned *v = nullptr, *v2 = nullptr, *gofs = nullptr;
@@ -680,9 +690,9 @@ int gb_radix_lookback_timeout_probe(GbCtx& c, int spin_limit) {
   cudaMemsetAsync(status, 0, 2 * 256 * 8, c.stream);
   cudaMemsetAsync(gofs, 0, 256 * 4, c.stream);
   k_rs_set_counter<<<1, 1, 0, c.stream>>>(ctr, 1);
-  const size_t smem = rs_smem_bytes(IT, 256);
-  cudaFuncSetAttribute((const void*)k_rs_pass<IT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_rs_pass<IT, 8><<<1, RS_THREADS, smem, c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st, spin_limit,
+  const size_t smem = rs_smem_bytes(NT, IT, 256);
+  cudaFuncSetAttribute((const void*)k_rs_pass<NT, IT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_rs_pass<NT, IT, 8><<<1, NT, smem, c.stream>>>(k, v, k2, v2, n, 0, 8, gofs, status, 7, ctr, c.st, spin_limit,
                                                    1);
   const cudaError_t e = cudaStreamSynchronize(c.stream);
   cudaFree(k); cudaFree(k2); cudaFree(v); cudaFree(v2); cudaFree(status); cudaFree(gofs); cudaFree(ctr);

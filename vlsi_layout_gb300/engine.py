@@ -279,13 +279,13 @@ class Context:
         self._chk(lib().gb_canonical_sort(self.h, b.ctypes.data, len(b)))
         return b
 
-    def radix_sort_device(self, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes=0, items=0):
+    def radix_sort_device(self, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes=0, tile=0):
         """Sort n device (uint64 key, uint32 value) pairs in place by the low
-        `bits` key bits (asynchronous on the context stream).  passes/items 0:
+        `bits` key bits (asynchronous on the context stream).  passes/tile 0:
         the tuned or default configuration.  Returns the pass count."""
         L = lib()
-        if passes or items:
-            r = L.gb_radix_sort_device_cfg(self.h, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes, items)
+        if passes or tile:
+            r = L.gb_radix_sort_device_cfg(self.h, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp, passes, tile)
         else:
             r = L.gb_radix_sort_device(self.h, keys_ptr, vals_ptr, n, bits, keys_tmp, vals_tmp)
         if r < 0:
@@ -295,7 +295,7 @@ class Context:
     def radix_autotune(self, keys_ptr, vals_ptr, n, bits):
         """Time the built sort configurations on a copy of the pairs; the
         fastest is used by later sorts of this size class.  Returns
-        (passes, items, ms)."""
+        (passes, tile keys, ms)."""
         p, it, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
         self._chk(lib().gb_radix_autotune(self.h, keys_ptr, vals_ptr, n, bits, ctypes.byref(p), ctypes.byref(it),
                                           ctypes.byref(ms)))
