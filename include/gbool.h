@@ -51,6 +51,8 @@ extern "C" {
 #define GB_OP_NOT 3   /* A - B */
 #define GB_OP_MERGE 4 /* union of A */
 #define GB_OP_SIZE 5  /* PerformBoostPolygonOperation only: resize by control_value */
+#define GB_OP_OVERLAP 7 /* single-layer AND (CalculateSingleLayerAND, design_impl.f90:385-498):
+                           the area covered by at least two boxes of A; B unused */
 
 /* AoS box, identical to c_box of boost_polygon_api.h:16-23 and Fortran type(Box). */
 struct c_box {
@@ -144,7 +146,9 @@ int gb_layer_to_host(gb_context* ctx, gb_layer* L, c_box* out, unsigned long lon
                      unsigned long long* n, long long* cell_offsets);
 void gb_layer_free(gb_context* ctx, gb_layer* L);
 
-/* Operators (device-resident, asynchronous on the context stream). */
+/* Operators (device-resident, asynchronous on the context stream).
+ * gb_op_bool: op GB_OP_XOR/OR/AND/NOT need B; GB_OP_MERGE and GB_OP_OVERLAP
+ * take A alone (B ignored). */
 int gb_op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, gb_layer** out);
 int gb_op_grow(gb_context* ctx, gb_layer* A, int32_t E, int32_t N, int32_t W, int32_t S,
                gb_layer** out);
@@ -157,6 +161,24 @@ int gb_op_area(gb_context* ctx, gb_layer* A, long long* area_per_cell);
  * roots numbered in index order). */
 int gb_components(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* ncomp,
                   long long* labels);
+
+/* Overlap statistics of n host boxes (ComputeInteractionsCPU and
+ * FindSingletonsCPU, pnummerge.f90:388-562): *strict_pairs = pairs i<k whose
+ * boxes overlap with positive area; *singletons = boxes that no other box
+ * touches or overlaps (closed bounds); is_singleton (optional, n bytes) gets
+ * the mask.  Either count pointer may be NULL.  Synchronous. */
+int gb_interactions(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* strict_pairs,
+                    long long* singletons, unsigned char* is_singleton);
+/* CertifyHealing (design_impl.f90:35-56): *healed = 1 when n < 2 or no two
+ * boxes overlap with positive area, else 0. */
+int gb_certify_healing(gb_context* ctx, const c_box* boxes, unsigned long long n, int* healed);
+/* Union area per PNUM component (calculate_union_area_by_polygon,
+ * design.f90:854-935): areas[0] = total area of the singletons, areas[k] =
+ * union area of component k (labels as gb_components), k = 1..R.  *nlabels
+ * receives R + 1; GB_ERR_CAPACITY when cap < R + 1 (areas may then be NULL
+ * to size the call).  Their sum is the union area of the layer. */
+int gb_component_areas(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* areas,
+                       unsigned long long cap, long long* nlabels);
 
 /* Morton-key sort of n host boxes: keys_out (optional) and perm (optional,
  * 0-based) receive the sorted keys and the permutation; boxes are sorted in

@@ -23,12 +23,15 @@ struct Box { int32_t x1, y1, x2, y2; };
 
 inline bool valid(const Box& b) { return b.x1 < b.x2 && b.y1 < b.y2; }  // geometry.f90:66-70
 
-inline bool pred(int op, bool a, bool b) {
+// ca, cb: how many boxes of A and of B cover the point
+inline bool pred(int op, int32_t ca, int32_t cb) {
+  const bool a = ca > 0, b = cb > 0;
   switch (op) {
     case ORC_XOR: return a != b;
     case ORC_OR: return a || b;
     case ORC_AND: return a && b;
     case ORC_NOT: return a && !b;
+    case ORC_OVERLAP: return ca >= 2;  // CalculateSingleLayerAND, design_impl.f90:385-498
     default: return a;  // ORC_MERGE
   }
 }
@@ -78,7 +81,7 @@ void sweep_tile(const std::vector<Piece>& pcs, int op, std::vector<Box>& out) {
     for (const auto& kv : lap) {
       ca += kv.second.first;
       cb += kv.second.second;
-      const bool now = pred(op, ca > 0, cb > 0);
+      const bool now = pred(op, ca, cb);
       if (!in && now) { ys = kv.first; in = true; }
       else if (in && !now) { curr.push_back({ys, kv.first, X}); in = false; }
     }
@@ -135,7 +138,7 @@ int64_t boolean_impl(const Box* A, int64_t nA, const Box* B, int64_t nB, int op,
       }
   };
   for (int64_t i = 0; i < nA; ++i) add(A[i], 0);
-  if (op != ORC_MERGE)
+  if (op != ORC_MERGE && op != ORC_OVERLAP)
     for (int64_t i = 0; i < nB; ++i) add(B[i], 1);
   const int64_t nt = (int64_t)tiles.size();
   std::vector<std::vector<Box>> outs(nt);
@@ -316,6 +319,62 @@ int64_t orc_components(const orc_box* Ab, int64_t n, int64_t* labels) {
     for (int64_t i = 0; i < n; ++i)
       if (touched[i]) labels[i] = map[find(i)];
   return comps;
+}
+
+// ComputeInteractionsCPU (pnummerge.f90:483-562) counts the pairs i<k whose
+// boxes overlap with strict bounds (<) on both axes; FindSingletonsCPU
+// (:388-482) marks a box as a singleton unless another box meets it with
+// closed bounds (<=).  Candidates come from an x1-sorted sweep.
+void orc_interactions(const orc_box* Ab, int64_t n, int64_t* pairs, int64_t* singletons, uint8_t* is_singleton) {
+  const Box* A = (const Box*)Ab;
+  int64_t np = 0;
+  std::vector<uint8_t> touched(n > 0 ? n : 0, 0);
+  if (n > 0) {
+    std::vector<int64_t> ord(n);
+    for (int64_t i = 0; i < n; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
+      return A[a].x1 != A[b].x1 ? A[a].x1 < A[b].x1 : a < b;
+    });
+    for (int64_t s = 0; s < n; ++s) {
+      const Box& bi = A[ord[s]];
+      for (int64_t t = s + 1; t < n && A[ord[t]].x1 <= bi.x2; ++t) {
+        const Box& bk = A[ord[t]];
+        if (std::max(bi.y1, bk.y1) <= std::min(bi.y2, bk.y2)) {
+          touched[ord[s]] = touched[ord[t]] = 1;
+          if (std::max(bi.x1, bk.x1) < std::min(bi.x2, bk.x2) && std::max(bi.y1, bk.y1) < std::min(bi.y2, bk.y2))
+            ++np;
+        }
+      }
+    }
+  }
+  int64_t ns = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    ns += touched[i] ? 0 : 1;
+    if (is_singleton) is_singleton[i] = touched[i] ? 0 : 1;
+  }
+  if (pairs) *pairs = np;
+  if (singletons) *singletons = ns;
+}
+
+// calculate_union_area_by_polygon (design.f90:854-935): boxes grouped by PNUM
+// number; the singletons (number 0) add their own areas, every other group
+// adds the union area of its boxes (calculate_union_area_fast).
+int64_t orc_component_areas(const orc_box* A, int64_t n, int64_t* areas) {
+  if (n <= 0) {
+    if (areas) areas[0] = 0;
+    return 0;
+  }
+  std::vector<int64_t> lab(n);
+  orc_components(A, n, lab.data());
+  int64_t R = 0;
+  for (int64_t i = 0; i < n; ++i) R = std::max(R, lab[i]);
+  if (!areas) return R;
+  std::vector<std::vector<orc_box>> groups(R + 1);
+  for (int64_t i = 0; i < n; ++i) groups[lab[i]].push_back(A[i]);
+  areas[0] = 0;
+  for (const orc_box& b : groups[0]) areas[0] += (int64_t)(b.x2 - b.x1) * (b.y2 - b.y1);
+  for (int64_t k = 1; k <= R; ++k) areas[k] = orc_union_area(groups[k].data(), (int64_t)groups[k].size());
+  return R;
 }
 
 // ComputeMorton (gpu_morton.cu:113-144): centre = ((int64)x1+x2)/2 truncated,

@@ -39,7 +39,9 @@ extern "C" {
 
 typedef struct { int32_t x1, y1, x2, y2; } orc_box;
 
-enum { ORC_XOR = 0, ORC_OR = 1, ORC_AND = 2, ORC_NOT = 3, ORC_MERGE = 4 };
+enum { ORC_XOR = 0, ORC_OR = 1, ORC_AND = 2, ORC_NOT = 3, ORC_MERGE = 4, ORC_OVERLAP = 7 };
+/* ORC_OVERLAP: single-layer AND, the area covered by at least two boxes of A
+ * (B unused). */
 
 /* Canonical strips of pred(A, B) (op as above).  *out is malloc'd (free with
  * orc_free).  Returns the strip count, or -1 on invalid input boxes. */
@@ -57,6 +59,19 @@ int64_t orc_union_area(const orc_box* A, int64_t n);
  * 1..R with roots numbered in index order.  Returns the component count
  * (non-singleton components + singletons). */
 int64_t orc_components(const orc_box* A, int64_t n, int64_t* labels);
+/* Overlap statistics of one layer: *pairs = pairs i<k whose boxes overlap
+ * with positive area (ComputeInteractionsCPU, pnummerge.f90:483-562);
+ * *singletons = boxes with no other box touching or overlapping them
+ * (closed bounds, FindSingletonsCPU, pnummerge.f90:388-482); is_singleton
+ * (optional, n entries) gets the mask. */
+void orc_interactions(const orc_box* A, int64_t n, int64_t* pairs, int64_t* singletons,
+                      uint8_t* is_singleton);
+/* Union area per PNUM component (calculate_union_area_by_polygon,
+ * design.f90:854-935): areas[0] = total area of the singletons, areas[k] =
+ * union area of component k (labels of orc_components).  Returns R, the
+ * number of non-singleton components (areas holds R + 1 entries; pass
+ * areas = NULL to size it). */
+int64_t orc_component_areas(const orc_box* A, int64_t n, int64_t* areas);
 uint64_t orc_morton_key(const orc_box* b);
 uint64_t orc_tracker_key(int32_t X, int32_t Y);
 int32_t orc_um_to_dbu(double r);

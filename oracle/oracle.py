@@ -17,6 +17,7 @@ _LIB = os.path.join(_HERE, "_build", "libgbo_oracle.so")
 _REF = os.path.join(_HERE, "_ref", "libref_sort.so")
 
 XOR, OR, AND, NOT, MERGE = 0, 1, 2, 3, 4
+OVERLAP = 7  # single-layer AND: area covered by at least two boxes
 
 _lib = None
 
@@ -46,6 +47,10 @@ def lib():
         L.orc_union_area.restype = i64
         L.orc_components.argtypes = [P, i64, P]
         L.orc_components.restype = i64
+        L.orc_interactions.argtypes = [P, i64, P, P, P]
+        L.orc_interactions.restype = None
+        L.orc_component_areas.argtypes = [P, i64, P]
+        L.orc_component_areas.restype = i64
         L.orc_morton_key.argtypes = [P]
         L.orc_morton_key.restype = ctypes.c_uint64
         L.orc_tracker_key.argtypes = [i32, i32]
@@ -114,6 +119,30 @@ def components(A):
     labels = np.zeros(len(A), np.int64)
     n = lib().orc_components(A.ctypes.data, len(A), labels.ctypes.data)
     return int(n), labels
+
+
+def overlap(A, grid_log2=16):
+    """Single-layer AND (design_impl.f90:385-498) as canonical strips of the
+    area covered by at least two boxes of A."""
+    return boolean(A, np.zeros((0, 4), np.int32), OVERLAP, grid_log2)
+
+
+def interactions(A):
+    """(strict overlap pairs, singletons, singleton mask) of one layer."""
+    A = _arr(A)
+    pairs, singles = ctypes.c_int64(), ctypes.c_int64()
+    mask = np.zeros(len(A), np.uint8)
+    lib().orc_interactions(A.ctypes.data, len(A), ctypes.byref(pairs), ctypes.byref(singles), mask.ctypes.data)
+    return int(pairs.value), int(singles.value), mask
+
+
+def component_areas(A):
+    """Union area per PNUM component: [singleton area, area of component 1, ...]."""
+    A = _arr(A)
+    R = int(lib().orc_component_areas(A.ctypes.data, len(A), None))
+    out = np.zeros(R + 1, np.int64)
+    lib().orc_component_areas(A.ctypes.data, len(A), out.ctypes.data)
+    return out
 
 
 def morton_keys(A):

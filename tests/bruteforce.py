@@ -6,14 +6,18 @@ persist unchanged across consecutive x-slabs (the heal_boxes form)."""
 import numpy as np
 
 
-def _pred(op, a, b):
+def _pred(op, ca, cb):
+    """ca, cb: per-cell coverage counts of A and B."""
+    if op == 7:  # single-layer AND: covered at least twice
+        return ca >= 2
+    a, b = ca > 0, cb > 0
     return [a ^ b, a | b, a & b, a & ~b, a][op]
 
 
 def canonical(A, B, op, g=16):
     A = np.asarray(A, np.int64).reshape(-1, 4)
     B = np.asarray(B, np.int64).reshape(-1, 4)
-    allb = np.concatenate([A, B]) if op != 4 else A
+    allb = np.concatenate([A, B]) if op not in (4, 7) else A
     if len(allb) == 0:
         return np.zeros((0, 4), np.int32)
     xs = set(allb[:, 0]) | set(allb[:, 2])
@@ -27,11 +31,11 @@ def canonical(A, B, op, g=16):
     ys = np.array(sorted(ys))
     cov = {}
     for name, S in (("a", A), ("b", B)):
-        m = np.zeros((len(xs) - 1, len(ys) - 1), bool)
+        m = np.zeros((len(xs) - 1, len(ys) - 1), np.int32)
         for x1, y1, x2, y2 in S:
             i1, i2 = np.searchsorted(xs, x1), np.searchsorted(xs, x2)
             j1, j2 = np.searchsorted(ys, y1), np.searchsorted(ys, y2)
-            m[i1:i2, j1:j2] = True
+            m[i1:i2, j1:j2] += 1
         cov[name] = m
     R = _pred(op, cov["a"], cov["b"])
     out = []

@@ -80,7 +80,7 @@ def test_complement_identity(oracle):
     assert oracle.area_of(comp) == box_area - oracle.union_area(b)
 
 
-@pytest.mark.parametrize("op", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("op", [0, 1, 2, 3, 4, 7])
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_oracle_matches_bruteforce(oracle, op, seed):
     A = random_layer(40, die=3000, wmin=5, wmax=600, seed=seed, x0=-1500)
@@ -129,3 +129,52 @@ def test_components_semantics(oracle):
     assert n == 1 and lab.tolist() == [0]
     n, lab = oracle.components([[10, 10, 20, 20], [0, 0, 5, 5], [4, 4, 11, 11]])
     assert n == 1 and lab.tolist() == [1, 1, 1]
+
+
+def test_overlap_semantics(oracle):
+    # CalculateSingleLayerAND (design_impl.f90:385-498): positive-area pairwise
+    # intersections, as a point set the area covered at least twice
+    A = [[0, 0, 10, 10], [5, 5, 15, 15], [10, 0, 20, 5], [30, 30, 40, 40], [30, 30, 40, 40]]
+    assert oracle.overlap(A).tolist() == [[5, 5, 10, 10], [30, 30, 40, 40]]
+    assert len(oracle.overlap([[0, 0, 1, 1], [1, 0, 2, 1]])) == 0  # edge touch only
+    B = random_layer(3000, die=300000, seed=21)
+    # a healed layer overlaps nowhere; overlap lies inside the union
+    assert len(oracle.overlap(oracle.merge(B))) == 0
+    assert len(oracle.boolean(oracle.overlap(B), oracle.merge(B), oracle.NOT)) == 0
+
+
+def _pairs_brute(A):
+    A = np.asarray(A, np.int64)
+    n = len(A)
+    strict = 0
+    touched = np.zeros(n, bool)
+    for i in range(n):
+        for k in range(i + 1, n):
+            ox = max(A[i, 0], A[k, 0]), min(A[i, 2], A[k, 2])
+            oy = max(A[i, 1], A[k, 1]), min(A[i, 3], A[k, 3])
+            if ox[0] <= ox[1] and oy[0] <= oy[1]:
+                touched[i] = touched[k] = True
+                strict += ox[0] < ox[1] and oy[0] < oy[1]
+    return strict, int((~touched).sum()), (~touched).astype(np.uint8)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_interactions_match_bruteforce(oracle, seed):
+    # ComputeInteractionsCPU (pnummerge.f90:483-562, strict <) and
+    # FindSingletonsCPU (:388-482, closed <=)
+    A = random_layer(300, die=20000, wmin=5, wmax=900, seed=seed)
+    A = np.concatenate([A, A[:5], [[0, 0, 10, 10], [10, 0, 20, 10], [20, 10, 30, 20]]]).astype(np.int32)
+    p, s, m = oracle.interactions(A)
+    ep, es, em = _pairs_brute(A)
+    assert (p, s) == (ep, es) and m.tolist() == em.tolist()
+    # a healed layer certifies: no strict pairs
+    assert oracle.interactions(oracle.merge(A))[0] == 0
+
+
+def test_component_areas(oracle):
+    A = [[0, 0, 10, 10], [5, 5, 15, 15], [20, 0, 30, 10], [30, 0, 40, 10], [100, 100, 110, 110]]
+    assert oracle.component_areas(A).tolist() == [100, 175, 200]
+    B = random_layer(5000, die=400000, seed=9)
+    ar = oracle.component_areas(B)
+    n, lab = oracle.components(B)
+    assert len(ar) == lab.max() + 1 and ar.sum() == oracle.union_area(B)

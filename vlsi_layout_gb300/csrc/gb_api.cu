@@ -555,8 +555,9 @@ gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode) {
   GbCtx& c = ctx->c;
   const int g = 16;
   gb_layer* Ab = binned_of(ctx, A, g);
-  gb_layer* Bb = (B && op != GB_OP_MERGE) ? binned_of(ctx, B, g) : nullptr;
-  if (!Ab || (B && op != GB_OP_MERGE && !Bb)) return nullptr;
+  const bool single = op == GB_OP_MERGE || op == GB_OP_OVERLAP;
+  gb_layer* Bb = (B && !single) ? binned_of(ctx, B, g) : nullptr;
+  if (!Ab || (B && !single && !Bb)) return nullptr;
   gb_layer* O = new_arena_layer(ctx, A->ncell, g);
   if (!O) return nullptr;
   gb_launch_bool_setup(c, op, Ab->d, Bb ? Bb->d : nullptr, O->d, A->ncell, g, mode == 0);
@@ -567,8 +568,10 @@ gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode) {
 
 extern "C" int gb_op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, gb_layer** out) {
   if (!ctx || !A || !out || A->dead || (B && B->dead)) return GB_ERR_ARG;
-  if (op < GB_OP_XOR || op > GB_OP_MERGE) return GB_ERR_ARG;
-  if (op != GB_OP_MERGE && !B) return GB_ERR_ARG;
+  if ((op < GB_OP_XOR || op > GB_OP_MERGE) && op != GB_OP_OVERLAP) return GB_ERR_ARG;
+  const bool single = op == GB_OP_MERGE || op == GB_OP_OVERLAP;
+  if (!single && !B) return GB_ERR_ARG;
+  if (single) B = nullptr;
   if (B && B->ncell != A->ncell) return set_err(ctx, GB_ERR_ARG, "operands differ in cell count");
   *out = op_bool(ctx, op, A, B, 0);
   return *out ? GB_OK : set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
@@ -663,6 +666,18 @@ int run_retry(gb_context* ctx, F&& body) {
 int gb_run_retry(gb_context* ctx, const std::function<int()>& body) { return run_retry(ctx, body); }
 
 // ======================================================================= connectivity
+// Grid for candidate pairs of a one-cell raw layer: about 32 boxes per tile.
+static int pair_grid(gb_context* ctx, gb_layer* L, long long n) {
+  DLayer d = read_desc(ctx, L);
+  int4 bb;
+  cudaMemcpy(&bb, d.cbox, 16, cudaMemcpyDeviceToHost);
+  const double W = (double)bb.z - bb.x + 1, H = (double)bb.w - bb.y + 1;
+  const double cell = std::sqrt(W * H * 32.0 / (double)(n > 0 ? n : 1));
+  int g = 4;
+  while (g < 30 && (double)(1ll << g) < cell) ++g;
+  return g;
+}
+
 extern "C" int gb_components(gb_context* ctx, const c_box* boxes, unsigned long long n,
                              long long* ncomp, long long* labels) {
   if (!ctx || !ncomp) return GB_ERR_ARG;
@@ -674,14 +689,7 @@ extern "C" int gb_components(gb_context* ctx, const c_box* boxes, unsigned long 
   if (e) return e;
   e = gb_sync(ctx, nullptr);
   if (e) { gb_layer_free(ctx, L); return e; }
-  DLayer d = read_desc(ctx, L);
-  int4 bb;
-  cudaMemcpy(&bb, d.cbox, 16, cudaMemcpyDeviceToHost);
-  // grid for candidate pairs: about 32 boxes per tile, never finer than the mean box size
-  const double W = (double)bb.z - bb.x + 1, H = (double)bb.w - bb.y + 1;
-  double cell = std::sqrt(W * H * 32.0 / (double)n);
-  int g = 4;
-  while (g < 30 && (double)(1ll << g) < cell) ++g;
+  const int g = pair_grid(ctx, L, (long long)n);
   int* parent = nullptr;
   unsigned char* touched = nullptr;
   long long* lab = nullptr;
@@ -710,6 +718,168 @@ extern "C" int gb_components(gb_context* ctx, const c_box* boxes, unsigned long 
     }
   }
   cudaFree(parent); cudaFree(touched); cudaFree(lab); cudaFree(map); cudaFree(flag); cudaFree(nc);
+  gb_layer_free(ctx, L);
+  return e;
+}
+
+// ComputeInteractions / FindSingletons (pnummerge.f90:388-562) and
+// CertifyHealing (design_impl.f90:35-56) on the GPU.
+extern "C" int gb_interactions(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* strict_pairs,
+                               long long* singletons, unsigned char* is_singleton) {
+  if (!ctx || (n && !boxes)) return GB_ERR_ARG;
+  if (n > 0x7fffffffull) return set_err(ctx, GB_ERR_ARG, "too many boxes for int32 indices");
+  if (n == 0) {
+    if (strict_pairs) *strict_pairs = 0;
+    if (singletons) *singletons = 0;
+    return GB_OK;
+  }
+  GbCtx& c = ctx->c;
+  gb_layer* L = nullptr;
+  int e = gb_layer_from_host(ctx, boxes, n, nullptr, 1, &L);
+  if (e) return e;
+  e = gb_sync(ctx, nullptr);
+  if (e) { gb_layer_free(ctx, L); return e; }
+  const int g = pair_grid(ctx, L, (long long)n);
+  unsigned char* touched = nullptr;
+  unsigned char* mask = nullptr;
+  unsigned long long* cnt = nullptr;
+  cudaMalloc(&touched, n);
+  cudaMalloc(&cnt, 16);
+  if (is_singleton) cudaMalloc(&mask, n);
+  if (!touched || !cnt || (is_singleton && !mask)) {
+    e = set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in gb_interactions");
+  } else {
+    e = run_retry(ctx, [&]() -> int {
+      gb_layer* B = new_arena_layer(ctx, 1, g);
+      if (!B) return GB_ERR_CAPACITY;
+      gb_launch_bin_index(c, L->d, B->d, 1, g);
+      gb_launch_pair_stats(c, L->d, B->d, g, touched, (long long)n, cnt, cnt + 1, mask);
+      return GB_OK;
+    });
+    if (e == GB_OK) {
+      unsigned long long h[2];
+      cudaMemcpy(h, cnt, 16, cudaMemcpyDeviceToHost);
+      if (strict_pairs) *strict_pairs = (long long)h[0];
+      if (singletons) *singletons = (long long)h[1];
+      if (is_singleton) cudaMemcpy(is_singleton, mask, n, cudaMemcpyDeviceToHost);
+    }
+  }
+  cudaFree(touched); cudaFree(mask); cudaFree(cnt);
+  gb_layer_free(ctx, L);
+  return e;
+}
+
+extern "C" int gb_certify_healing(gb_context* ctx, const c_box* boxes, unsigned long long n, int* healed) {
+  if (!ctx || !healed) return GB_ERR_ARG;
+  if (n < 2) { *healed = 1; return GB_OK; }
+  long long pairs = 0;
+  const int e = gb_interactions(ctx, boxes, n, &pairs, nullptr, nullptr);
+  if (!e) *healed = pairs == 0 ? 1 : 0;
+  return e;
+}
+
+__global__ void k_label_keys(const long long* lab, long long n, unsigned long long* keys, unsigned* vals) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    keys[i] = (unsigned long long)lab[i];
+    vals[i] = (unsigned)i;
+  }
+}
+
+// off[l] = first position of label l in the label-sorted keys, off[R+1] = n
+// (labels 1..R all occur; label 0 may not).
+__global__ void k_label_offsets(const unsigned long long* keys, long long n, long long R, long long* off) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long prev = i == 0 ? -1 : (long long)keys[i - 1];
+    const long long cur = i == n ? R + 1 : (long long)keys[i];
+    for (long long l = prev + 1; l <= cur; ++l) off[l] = i;
+  }
+}
+
+// Union area per PNUM component (calculate_union_area_by_polygon,
+// design.f90:854-935): the boxes are grouped by component label on the
+// device (labels of gb_components, radix-sorted), each group becomes one cell
+// of a layer, and the per-cell union area is the component's area; cell 0
+// holds the singletons, whose boxes are disjoint.
+extern "C" int gb_component_areas(gb_context* ctx, const c_box* boxes, unsigned long long n, long long* areas,
+                                  unsigned long long cap, long long* nlabels) {
+  if (!ctx || !nlabels || (n && !boxes)) return GB_ERR_ARG;
+  if (n > 0x7fffffffull) return set_err(ctx, GB_ERR_ARG, "too many boxes for int32 indices");
+  if (n == 0) {
+    *nlabels = 1;
+    if (cap < 1) return GB_ERR_CAPACITY;
+    if (areas) areas[0] = 0;
+    return GB_OK;
+  }
+  GbCtx& c = ctx->c;
+  gb_layer* L = nullptr;
+  int e = gb_layer_from_host(ctx, boxes, n, nullptr, 1, &L);
+  if (e) return e;
+  e = gb_sync(ctx, nullptr);
+  if (e) { gb_layer_free(ctx, L); return e; }
+  const int g = pair_grid(ctx, L, (long long)n);
+  int* parent = nullptr;
+  unsigned char* touched = nullptr;
+  long long *lab = nullptr, *map = nullptr, *nc = nullptr, *off = nullptr;
+  int* flag = nullptr;
+  unsigned long long *keys = nullptr, *kt = nullptr;
+  unsigned *vals = nullptr, *vt = nullptr;
+  int4* sorted = nullptr;
+  cudaMalloc(&parent, n * 4);
+  cudaMalloc(&touched, n);
+  cudaMalloc(&lab, n * 8);
+  cudaMalloc(&map, n * 8);
+  cudaMalloc(&flag, n * 4);
+  cudaMalloc(&nc, 8);
+  cudaMalloc(&keys, n * 8);
+  cudaMalloc(&kt, n * 8);
+  cudaMalloc(&vals, n * 4);
+  cudaMalloc(&vt, n * 4);
+  cudaMalloc(&sorted, n * 16);
+  gb_layer* G = nullptr;
+  if (!parent || !touched || !lab || !map || !flag || !nc || !keys || !kt || !vals || !vt || !sorted) {
+    e = set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in gb_component_areas");
+  } else {
+    e = run_retry(ctx, [&]() -> int {
+      gb_layer* B = new_arena_layer(ctx, 1, g);
+      if (!B) return GB_ERR_CAPACITY;
+      gb_launch_bin_index(c, L->d, B->d, 1, g);
+      gb_launch_components(c, L->d, B->d, parent, touched, lab, (long long)n, nc, flag, map);
+      return GB_OK;
+    });
+  }
+  long long R = 0;
+  if (e == GB_OK) {
+    long long ncomp = 0, nsingle = 0;
+    cudaMemcpy(&ncomp, nc, 8, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&nsingle, c.dscal + 4, 8, cudaMemcpyDeviceToHost);
+    R = ncomp - nsingle;
+    *nlabels = R + 1;
+    if (cap < (unsigned long long)(R + 1)) e = GB_ERR_CAPACITY;
+  }
+  if (e == GB_OK) {
+    cudaMalloc(&off, (size_t)(R + 2) * 8);
+    if (!off) e = set_err(ctx, GB_ERR_OOM, "cudaMalloc failed in gb_component_areas");
+  }
+  if (e == GB_OK) {
+    int bits = 1;
+    while (bits < 63 && (R >> bits)) ++bits;
+    k_label_keys<<<c.work_blocks, 256, 0, c.stream>>>(lab, (long long)n, keys, vals);
+    if (gb_radix_sort_pairs(c, keys, vals, (long long)n, bits, kt, vt) < 0)
+      e = set_err(ctx, GB_ERR_INTERNAL, "radix sort setup failed");
+  }
+  if (e == GB_OK) {
+    k_gather_boxes<<<c.work_blocks, 256, 0, c.stream>>>((const int4*)L->own_boxes, vals, sorted, (long long)n);
+    k_label_offsets<<<c.work_blocks, 256, 0, c.stream>>>(keys, (long long)n, R, off);
+    c.launches += 3;
+    e = gb_sync(ctx, nullptr);
+    if (!e) e = gb_layer_from_device(ctx, (const c_box*)sorted, n, off, (int)(R + 1), &G);
+    if (!e) e = areas ? gb_op_area(ctx, G, areas) : GB_OK;
+  }
+  if (G) gb_layer_free(ctx, G);
+  cudaFree(parent); cudaFree(touched); cudaFree(lab); cudaFree(map); cudaFree(flag); cudaFree(nc);
+  cudaFree(keys); cudaFree(kt); cudaFree(vals); cudaFree(vt); cudaFree(sorted); cudaFree(off);
   gb_layer_free(ctx, L);
   return e;
 }

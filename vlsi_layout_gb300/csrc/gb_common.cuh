@@ -35,6 +35,9 @@
 #define GB_OP_AND 2
 #define GB_OP_NOT 3
 #define GB_OP_MERGE 4
+// No Boost counterpart: single-layer AND (design_impl.f90:385-498), the area
+// covered by at least two boxes of A.
+#define GB_OP_OVERLAP 7
 
 #define GB_MAX_TILES_PER_OP (1ll << 28)
 

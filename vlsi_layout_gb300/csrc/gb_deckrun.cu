@@ -10,7 +10,8 @@
 // nothing`).  `exec run LHS = RHS1 OP RHS2 [args]` dispatches the operators of
 // controlparser.f90:442-585 to device-resident layers:
 //   + OR, * AND, @ ~ ! NOT / FRAMENOT, ^ XOR (abort_on_xor), % no-op,
-//   OR2 AND2 NOT FRAMENOT XOR, GROW e n w s, SIZE r, EXTENT, COPY,
+//   OR2 AND2 NOT FRAMENOT XOR, AND (single layer: covered twice), GROW e n w s,
+//   SIZE r, EXTENT, COPY,
 //   ASSERT_ZERO, WORMHOLE (no-op).
 // GROW / SIZE amounts are um, converted with int(1000*r) (truncation).  The
 // README's RUN_LOOP(`OP1', ...) macro line (op_template.m4) is expanded in
@@ -247,7 +248,12 @@ int exec_run(Deck& d, const std::string& rest) {
       return GB_ERR_ARG;
     }
   }
+  // a binary operator whose second operand is `nothing` sees an empty layer
+  // (the reference's init layer `t1:nothing` holds no boxes)
   auto need_b = [&]() {
+    if (!B && nothing) {
+      if (make_layer(d, {}, &B)) B = nullptr;
+    }
     if (!B) d.say("ERROR: operator %s needs a second layer (line %d)", op.c_str(), d.line_no);
     return B != nullptr;
   };
@@ -262,6 +268,8 @@ int exec_run(Deck& d, const std::string& rest) {
   } else if (op == "@" || op == "~" || op == "!" || op == "NOT" || op == "FRAMENOT") {
     if (!need_b()) return GB_ERR_ARG;
     e = gb_op_bool(d.ctx, GB_OP_NOT, A, B, &O);
+  } else if (op == "AND") {  // single-layer AND (controlparser.f90:545-549, design_impl.f90:385-498)
+    e = gb_op_bool(d.ctx, GB_OP_OVERLAP, A, nullptr, &O);
   } else if (op == "^" || op == "XOR") {
     if (!need_b()) return GB_ERR_ARG;
     e = gb_op_bool(d.ctx, GB_OP_XOR, A, B, &O);
@@ -321,7 +329,10 @@ int exec_run(Deck& d, const std::string& rest) {
     }
     e = make_layer(d, bb, &O);
   } else {
-    d.say("UNKNOWN primary_operator: %s on line: %d", op.c_str(), d.line_no);
+    if (op == "GRID")  // controlparser.f90:559-562 calls CreateGRID, which no source file defines
+      d.say("ERROR: GRID has no definition in the control language's sources (line %d)", d.line_no);
+    else
+      d.say("UNKNOWN primary_operator: %s on line: %d", op.c_str(), d.line_no);
     return GB_ERR_ARG;
   }
   if (e) {

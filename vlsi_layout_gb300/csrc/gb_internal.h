@@ -121,6 +121,13 @@ void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* pare
                           unsigned char* touched, long long* labels, long long n,
                           long long* out_ncomp_dev, int* flag_tmp, long long* map_tmp);
 
+// Overlap statistics of one layer: pairs overlapping with positive area
+// (*strict_dev) and boxes meeting no other box (*single_dev, mask_dev
+// optional).  binidx: closed-range index binning on grid g.
+void gb_launch_pair_stats(GbCtx& c, const DLayer* raw, DLayer* binidx, int g, unsigned char* touched,
+                          long long n, unsigned long long* strict_dev, unsigned long long* single_dev,
+                          unsigned char* mask_dev);
+
 // ---- radix sort (gb_radix.cu)
 // Sorts n (key, value) pairs by the low `bits` bits of the 64-bit keys.
 // tmp buffers must hold n entries each.  Stable.  passes / items (keys per

@@ -116,7 +116,22 @@ __device__ __forceinline__ unsigned long long gb_pred(int op, unsigned long long
     case GB_OP_XOR: return a ^ b;
     case GB_OP_AND: return a & b;
     case GB_OP_NOT: return a & ~b;
+    case GB_OP_OVERLAP: return b;  // b holds the rows covered a second time
     default: return a | b;  // OR, MERGE (B empty)
+  }
+}
+
+// Single-layer AND: a row bit painted into a column that already had it is
+// recorded in the second word array (atomics make the order of two paints of
+// the same cell irrelevant), so b ends as the cells covered at least twice.
+__device__ __forceinline__ void paint_twice(unsigned* a, unsigned* b, int c, unsigned mlo, unsigned mhi) {
+  if (mlo) {
+    const unsigned o = atomicOr(&a[2 * c], mlo) & mlo;
+    if (o) atomicOr(&b[2 * c], o);
+  }
+  if (mhi) {
+    const unsigned o = atomicOr(&a[2 * c + 1], mhi) & mhi;
+    if (o) atomicOr(&b[2 * c + 1], o);
   }
 }
 
@@ -250,9 +265,13 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       unsigned* col = (unsigned*)(own ? cb : ca);
       const unsigned mlo = (unsigned)mk, mhi = (unsigned)(mk >> 32);
       const int d = min(span, 4);
-      for (int c = lc1; c < lc1 + d; ++c) {
-        if (mlo) atomicOr(&col[2 * c], mlo);
-        if (mhi) atomicOr(&col[2 * c + 1], mhi);
+      if (op == GB_OP_OVERLAP) {
+        for (int c = lc1; c < lc1 + d; ++c) paint_twice((unsigned*)ca, (unsigned*)cb, c, mlo, mhi);
+      } else {
+        for (int c = lc1; c < lc1 + d; ++c) {
+          if (mlo) atomicOr(&col[2 * c], mlo);
+          if (mhi) atomicOr(&col[2 * c + 1], mhi);
+        }
       }
     }
     if (tctr) { const long long qb = clock64(); qsetup += qb - qa; qa = qb; }
@@ -277,8 +296,12 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         if (k < total) {
           unsigned* col = (unsigned*)(own_o ? cb : ca);
           const int c = c1_o + 4 + (k - ex_o);
-          if ((unsigned)mk_o) atomicOr(&col[2 * c], (unsigned)mk_o);
-          if ((unsigned)(mk_o >> 32)) atomicOr(&col[2 * c + 1], (unsigned)(mk_o >> 32));
+          if (op == GB_OP_OVERLAP) {
+            paint_twice((unsigned*)ca, (unsigned*)cb, c, (unsigned)mk_o, (unsigned)(mk_o >> 32));
+          } else {
+            if ((unsigned)mk_o) atomicOr(&col[2 * c], (unsigned)mk_o);
+            if ((unsigned)(mk_o >> 32)) atomicOr(&col[2 * c + 1], (unsigned)(mk_o >> 32));
+          }
         }
       }
     }
@@ -497,7 +520,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
           s.nA = A->tcount[ta];
           s.pa = A->pcs + A->tstart[ta];
         }
-        if (B && op != GB_OP_MERGE) {
+        if (B && op != GB_OP_MERGE && op != GB_OP_OVERLAP) {
           const int4 wb = B->win[k];
           if (tx >= wb.x && ty >= wb.y && tx < wb.x + wb.z && ty < wb.y + wb.w) {
             const long long tb = B->tbase[k] + (long long)(ty - wb.y) * wb.z + (tx - wb.x);

@@ -94,6 +94,73 @@ __global__ void __launch_bounds__(256) k_uf_tile(const DLayer* raw, const DLayer
   }
 }
 
+// Overlap statistics (ComputeInteractionsCPU, pnummerge.f90:483-562, and
+// FindSingletonsCPU, :388-482).  Every pair meeting with closed bounds marks
+// both boxes as non-singletons.  A pair overlapping with positive area is
+// counted once: in the tile holding the lower-left corner of its
+// intersection (both boxes are binned there, being closed-range binned).
+__device__ __forceinline__ bool strict_overlap(int4 a, int4 b) {
+  return max(a.x, b.x) < min(a.z, b.z) && max(a.y, b.y) < min(a.w, b.w);
+}
+
+__global__ void __launch_bounds__(256) k_pair_stats(const DLayer* raw, const DLayer* bin, int g,
+                                                    unsigned char* touched, unsigned long long* strict,
+                                                    long long* counter, DStatus* st) {
+  __shared__ int4 sb[UF_SMEM_BOXES];
+  __shared__ int si[UF_SMEM_BOXES];
+  __shared__ long long s_t;
+  const int4* boxes = raw->boxes;
+  const int* idx = (const int*)bin->pcs;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_t = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
+    __syncthreads();
+    const long long t = s_t;
+    if (t >= bin->ntiles) break;
+    const int k = bin->tcount[t];
+    if (k < 2) continue;
+    const int4 w = bin->win[0];
+    const long long li = t - bin->tbase[0];
+    const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+    const int* ti = idx + bin->tstart[t];
+    const bool in_smem = k <= UF_SMEM_BOXES;
+    if (in_smem) {
+      for (int j = threadIdx.x; j < k; j += blockDim.x) { si[j] = ti[j]; sb[j] = boxes[si[j]]; }
+      __syncthreads();
+    }
+    const int nw = blockDim.x >> 5;
+    unsigned long long cnt = 0;
+    for (int a = gb_warp(); a < k; a += nw) {
+      const int ia = in_smem ? si[a] : ti[a];
+      const int4 ba = in_smem ? sb[a] : boxes[ia];
+      for (int b = a + 1 + gb_lane(); b < k; b += 32) {
+        const int ib = in_smem ? si[b] : ti[b];
+        const int4 bb = in_smem ? sb[b] : boxes[ib];
+        if (closed_overlap(ba, bb)) {
+          touched[ia] = 1;
+          touched[ib] = 1;
+          if (strict_overlap(ba, bb) && (max(ba.x, bb.x) >> g) == tx && (max(ba.y, bb.y) >> g) == ty) ++cnt;
+        }
+      }
+    }
+    cnt = gb_warp_sum(cnt);
+    if (gb_lane() == 0 && cnt) atomicAdd(strict, cnt);
+  }
+}
+
+__global__ void k_singletons(const unsigned char* touched, long long n, unsigned char* mask,
+                             unsigned long long* nsingle) {
+  unsigned long long ns = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned char s = touched[i] ? 0 : 1;
+    if (mask) mask[i] = s;
+    ns += s;
+  }
+  ns = gb_warp_sum(ns);
+  if (gb_lane() == 0 && ns) atomicAdd(nsingle, ns);
+}
+
 __global__ void k_uf_flatten(int* parent, const unsigned char* touched, int* flag, long long n,
                              long long* nsingle) {
   long long ns = 0;
@@ -125,6 +192,18 @@ __global__ void k_set_ptrs(long long* slots, int* flag, long long* map, long lon
   slots[8] = (long long)flag;
   slots[9] = (long long)map;
   slots[10] = n;
+}
+
+void gb_launch_pair_stats(GbCtx& c, const DLayer* raw, DLayer* binidx, int g, unsigned char* touched,
+                          long long n, unsigned long long* strict_dev, unsigned long long* single_dev,
+                          unsigned char* mask_dev) {
+  cudaMemsetAsync(touched, 0, (size_t)n, c.stream);
+  cudaMemsetAsync(strict_dev, 0, 8, c.stream);
+  cudaMemsetAsync(single_dev, 0, 8, c.stream);
+  k_zero_ll<<<1, 32, 0, c.stream>>>(c.tile_counter + 1, 1);
+  k_pair_stats<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, g, touched, strict_dev, c.tile_counter + 1, c.st);
+  k_singletons<<<c.work_blocks, 256, 0, c.stream>>>(touched, n, mask_dev, single_dev);
+  c.launches += 3;
 }
 
 void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* parent,

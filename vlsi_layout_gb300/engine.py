@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libgbool.so")
 GB_OK, GB_ERR_CAPACITY, GB_ERR_INVALID_BOX, GB_ERR_OOM, GB_ERR_TIMEOUT, GB_ERR_CUDA, GB_ERR_ARG, \
     GB_ERR_INTERNAL = range(8)
 XOR, OR, AND, NOT, MERGE, SIZE = range(6)
+OVERLAP = 7  # single-layer AND: area covered by at least two boxes of A
 
 _ERRNAMES = {1: "CAPACITY", 2: "INVALID_BOX", 3: "OOM", 4: "TIMEOUT", 5: "CUDA", 6: "ARG", 7: "INTERNAL"}
 
@@ -95,6 +96,9 @@ def lib():
         "gb_radix_sort_device_cfg": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int]),
         "gb_radix_autotune": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P, P, P]),
         "gb_radix_tuning_reset": (None, []),
+        "gb_interactions": (ctypes.c_int, [P, P, u64, P, P, P]),
+        "gb_certify_healing": (ctypes.c_int, [P, P, u64, P]),
+        "gb_component_areas": (ctypes.c_int, [P, P, u64, P, u64, P]),
         "gb_morton_keys_device": (ctypes.c_int, [P, P, i64, P, P]),
         "gb_serve_create": (ctypes.c_int, [ctypes.c_int, u64, ctypes.c_int, u64, pp]),
         "gb_serve_add_layer": (ctypes.c_int, [P, P, u64, P]),
@@ -273,6 +277,33 @@ class Context:
         self._chk(lib().gb_profile_read(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(bi),
                                         ctypes.byref(bo)))
         return ms.value, n.value, bi.value, bo.value
+
+    def interactions(self, boxes):
+        """(strict overlap pairs, singletons, singleton mask) of host boxes."""
+        b = _boxes(boxes)
+        p, s = ctypes.c_int64(), ctypes.c_int64()
+        mask = np.zeros(len(b), np.uint8)
+        self._chk(lib().gb_interactions(self.h, b.ctypes.data, len(b), ctypes.byref(p), ctypes.byref(s),
+                                        mask.ctypes.data))
+        return p.value, s.value, mask
+
+    def certify_healing(self, boxes):
+        b = _boxes(boxes)
+        h = ctypes.c_int()
+        self._chk(lib().gb_certify_healing(self.h, b.ctypes.data, len(b), ctypes.byref(h)))
+        return bool(h.value)
+
+    def component_areas(self, boxes):
+        """Union area per component: [singleton area, component 1, ...]."""
+        b = _boxes(boxes)
+        nl = ctypes.c_int64()
+        r = lib().gb_component_areas(self.h, b.ctypes.data, len(b), None, 0, ctypes.byref(nl))
+        if r not in (GB_OK, GB_ERR_CAPACITY):
+            self._chk(r)
+        out = np.zeros(max(1, nl.value), np.int64)
+        self._chk(lib().gb_component_areas(self.h, b.ctypes.data, len(b), out.ctypes.data, len(out),
+                                           ctypes.byref(nl)))
+        return out[:nl.value]
 
     def canonical_sort(self, boxes):
         b = _boxes(boxes).copy()
