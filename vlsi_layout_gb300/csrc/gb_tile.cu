@@ -803,6 +803,20 @@ void gb_tile_setup(GbCtx& c) {
 
 __global__ void k_zero_counter(long long* ctr) { *ctr = 0; }
 
+// The output pool is sized for the worst case (cap_factor x input pieces) and
+// tiles reserve exactly what they emit.  When nothing was allocated in the
+// arena after the pool (no overflow, no scratch spill), the unused tail goes
+// back to the arena, so a chain of operators keeps only what it produced.
+__global__ void k_pool_trim(DLayer* O, DStatus* st) {
+  if (st->err || !O->pcs) return;
+  const unsigned long long start = (unsigned long long)((char*)O->pcs - st->arena_base);
+  const unsigned long long end = start + (((unsigned long long)O->npcs * 8ull + 255ull) & ~255ull);
+  if (st->arena_off != end || O->nused > O->npcs) return;
+  const long long used = O->nused > 0 ? O->nused : 0;
+  st->arena_off = start + (((unsigned long long)used * 8ull + 255ull) & ~255ull);
+  O->npcs = used;
+}
+
 void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode) {
   k_zero_counter<<<1, 1, 0, c.stream>>>(c.tile_counter);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -826,6 +840,10 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
                                                         c.tile_scr_bytes, c.tile_counter, c.st);
   if (c.prof) cudaEventRecordWithFlags(e1, c.stream, c.prof_flags);
   c.launches += 2;
+  if (mode == 0) {
+    k_pool_trim<<<1, 1, 0, c.stream>>>(O, c.st);
+    ++c.launches;
+  }
 }
 
 // ===================================================================== no-allocation entry point
