@@ -313,6 +313,7 @@ def main():
     ap.add_argument("--serve-rates", default="1000,10000")
     ap.add_argument("--sort-only", action="store_true")
     ap.add_argument("--sort-n", type=int, default=200_000_000)
+    ap.add_argument("--no-sort", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
     if args.sort_only:
@@ -455,6 +456,9 @@ def main():
     serving = None
     if rank == 0 and not args.no_serve:
         serving = serve_leg(rates=tuple(int(x) for x in args.serve_rates.split(",")))
+    sort = None
+    if rank == 0 and not args.no_sort:
+        sort = sort_leg(n=args.sort_n, steps=3)
     value = world * nbox / (ms / 1e3)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
@@ -482,6 +486,7 @@ def main():
         "assert_zero_failures": fails,
         "parity": parity,
         "serving": serving,
+        "sort": sort,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

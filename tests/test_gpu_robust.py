@@ -105,3 +105,21 @@ def test_invalid_boxes_are_rejected(ctx):
     assert ei.value.code == engine.GB_ERR_INVALID_BOX
     ctx.release(m)
     ctx.sync()
+
+
+def test_set_stream_leaves_caller_stream_alive():
+    """A context that adopted the caller's stream must not destroy it on close."""
+    torch = pytest.importorskip("torch")
+    from vlsi_layout_gb300 import engine
+    s = torch.cuda.Stream()
+    c = engine.Context(0)
+    c.set_stream(s.cuda_stream)
+    m = c.mark()
+    L = c.layer(random_layer(2000, die=50_000, seed=3))
+    assert c.op(engine.MERGE, L).count()[0] > 0
+    c.release(m)
+    c.close()
+    with torch.cuda.stream(s):
+        x = torch.arange(1000, device="cuda") * 2
+    s.synchronize()
+    assert int(x.sum().item()) == 999000

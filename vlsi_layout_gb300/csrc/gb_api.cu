@@ -328,15 +328,18 @@ extern "C" int gb_context_destroy(gb_context* ctx) {
   return GB_OK;
 }
 
+// The context destroys only a stream it created: adopting the caller's
+// stream releases the context's own one, and the caller keeps ownership.
 extern "C" int gb_set_stream(gb_context* ctx, void* stream) {
   if (!ctx) return GB_ERR_ARG;
-  cudaStreamSynchronize(ctx->c.stream);
-  if (stream) {
-    ctx->c.stream = (cudaStream_t)stream;
-  } else {
-    cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking);
-    ctx->c.own_stream = true;
-  }
+  GbCtx& c = ctx->c;
+  cudaStreamSynchronize(c.stream);
+  if (stream && (cudaStream_t)stream == c.stream) return GB_OK;
+  cudaStream_t next = (cudaStream_t)stream;
+  if (!next && cudaStreamCreateWithFlags(&next, cudaStreamNonBlocking) != cudaSuccess) return GB_ERR_CUDA;
+  if (c.own_stream) cudaStreamDestroy(c.stream);
+  c.stream = next;
+  c.own_stream = stream == nullptr;
   return GB_OK;
 }
 
