@@ -49,6 +49,7 @@
 #define TK_LVN 256
 #define TK_LCN 128
 #define TK_MW 64
+#define TK_LD 2     // independent global loads in flight per thread in the streaming loops
 #define KID_TILE 20
 
 // A strip piece of one sub-band, 16 bytes, stored downward from the top of
@@ -542,14 +543,27 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     // ---- A: tile ranks
     for (int w = tid; w < W; w += TK_NT) { s.xb[w] = 0; s.yb[w] = 0; }
     __syncthreads();
-    for (int i = tid; i < P; i += TK_NT) {
-      const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
-      int x1, y1, x2, y2;
-      gb_unpack(pk, x1, y1, x2, y2);
-      atomicOr(&s.xb[x1 >> 5], 1u << (x1 & 31));
-      atomicOr(&s.xb[x2 >> 5], 1u << (x2 & 31));
-      atomicOr(&s.yb[y1 >> 5], 1u << (y1 & 31));
-      atomicOr(&s.yb[y2 >> 5], 1u << (y2 & 31));
+    // pieces are read TK_LD at a time per thread, so their loads overlap
+    const unsigned long long* pa = s.pa;
+    const unsigned long long* pb = s.pb;
+    for (int i0 = tid; i0 < P; i0 += TK_LD * TK_NT) {
+      unsigned long long pk[TK_LD];
+#pragma unroll
+      for (int u = 0; u < TK_LD; ++u) {
+        const int i = i0 + u * TK_NT;
+        pk[u] = i < P ? (i < nA ? pa[i] : pb[i - nA]) : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < TK_LD; ++u) {
+        if (i0 + u * TK_NT < P) {
+          int x1, y1, x2, y2;
+          gb_unpack(pk[u], x1, y1, x2, y2);
+          atomicOr(&s.xb[x1 >> 5], 1u << (x1 & 31));
+          atomicOr(&s.xb[x2 >> 5], 1u << (x2 & 31));
+          atomicOr(&s.yb[y1 >> 5], 1u << (y1 & 31));
+          atomicOr(&s.yb[y2 >> 5], 1u << (y2 & 31));
+        }
+      }
     }
     __syncthreads();
     int Nx, Ny;
@@ -593,15 +607,28 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     for (int i = tid; i <= min(nsb, s.sbc == s.sbc_s ? TK_SBS : nsb); i += TK_NT) s.sbc[i] = 0;
     __syncthreads();
     if (!s.err) {
-      for (int i = tid; i < P; i += TK_NT) {
-        const unsigned long long pk = i < nA ? s.pa[i] : s.pb[i - nA];
-        int x1, y1, x2, y2;
-        gb_unpack(pk, x1, y1, x2, y2);
-        const int r1 = bm_rank2(s.xb, s.xp, x1), r2 = bm_rank2(s.xb, s.xp, x2);
-        const int c1 = bm_rank2(s.yb, s.yp, y1), c2 = bm_rank2(s.yb, s.yp, y2);
-        s.rk[i] = make_int4(r1, r2, c1, c2);
-        const int lo = r1 / 63, hi = min(nsb - 1, r2 / 63);
-        for (int q = lo; q <= hi; ++q) atomicAdd(&s.sbc[q], 1);
+      // warp-uniform trip count: the loop body uses warp-wide match / shuffles
+      for (int wb = tid & ~31; wb < P; wb += TK_LD * TK_NT) {
+        const int i0 = wb + gb_lane();
+        unsigned long long pk[TK_LD];
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u) {
+          const int i = i0 + u * TK_NT;
+          pk[u] = i < P ? (i < nA ? pa[i] : pb[i - nA]) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u) {
+          const int i = i0 + u * TK_NT;
+          if (i < P) {
+            int x1, y1, x2, y2;
+            gb_unpack(pk[u], x1, y1, x2, y2);
+            const int r1 = bm_rank2(s.xb, s.xp, x1), r2 = bm_rank2(s.xb, s.xp, x2);
+            const int c1 = bm_rank2(s.yb, s.yp, y1), c2 = bm_rank2(s.yb, s.yp, y2);
+            s.rk[i] = make_int4(r1, r2, c1, c2);
+            const int lo = r1 / 63, hi = min(nsb - 1, r2 / 63);
+            for (int q = lo; q <= hi; ++q) atomicAdd(&s.sbc[q], 1);
+          }
+        }
       }
     }
     __syncthreads();
@@ -641,11 +668,26 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     __syncthreads();
     if (!s.err) {
-      for (int i = tid; i < P; i += TK_NT) {
-        const int4 r = s.rk[i];
-        const int lo = r.x / 63, hi = min(nsb - 1, r.y / 63);
-        const int4 rec = make_int4(r.x | (i >= nA ? (int)0x80000000 : 0), r.y, r.z, r.w);
-        for (int q = lo; q <= hi; ++q) s.mem[atomicAdd(&s.sbc[q], 1)] = rec;
+      const int4* rkp = s.rk;
+      int4* memp = s.mem;
+      for (int wb = tid & ~31; wb < P; wb += TK_LD * TK_NT) {  // warp-uniform trip count
+        const int i0 = wb + gb_lane();
+        int4 rr[TK_LD];
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u) {
+          const int i = i0 + u * TK_NT;
+          rr[u] = i < P ? rkp[i] : make_int4(0, -1, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u) {
+          const int i = i0 + u * TK_NT;
+          if (i < P) {
+            const int4 r = rr[u];
+            const int lo = r.x / 63, hi = min(nsb - 1, r.y / 63);
+            const int4 rec = make_int4(r.x | (i >= nA ? (int)0x80000000 : 0), r.y, r.z, r.w);
+            for (int q = lo; q <= hi; ++q) memp[atomicAdd(&s.sbc[q], 1)] = rec;
+          }
+        }
       }
     }
     __syncthreads();
@@ -692,11 +734,31 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     if (prs)
       for (int sb = wid; sb < nsb; sb += TK_NW) {
         const int4 inf = s.sbinfo[sb];
-        for (int j = lane; j < inf.y; j += 32) PR[inf.x + j] = s.sbrec[sb][j];
+        const PieceRec* src = s.sbrec[sb];
+        for (int j0 = lane; j0 < inf.y; j0 += TK_LD * 32) {
+          PieceRec r[TK_LD];
+#pragma unroll
+          for (int u = 0; u < TK_LD; ++u)
+            if (j0 + u * 32 < inf.y) r[u] = src[j0 + u * 32];
+#pragma unroll
+          for (int u = 0; u < TK_LD; ++u)
+            if (j0 + u * 32 < inf.y) PR[inf.x + j0 + u * 32] = r[u];
+        }
       }
     if (xys) {
-      for (int i = tid; i < Nx; i += TK_NT) s.xyv[xyoff + i] = s.Xt[i];
-      for (int i = tid; i < Ny; i += TK_NT) s.xyv[xyoff + Nx + i] = s.Yt[i];
+      const int* xt = s.Xt;
+      const int* yt = s.Yt;
+      for (int i0 = tid; i0 < Nx + Ny; i0 += TK_LD * TK_NT) {
+        int v[TK_LD];
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u) {
+          const int i = i0 + u * TK_NT;
+          v[u] = i < Nx ? xt[i] : i < Nx + Ny ? yt[i - Nx] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < TK_LD; ++u)
+          if (i0 + u * TK_NT < Nx + Ny) s.xyv[xyoff + i0 + u * TK_NT] = v[u];
+      }
     }
     for (int p = tid; p < NP; p += TK_NT) succ[p] = -1;
     int H = 0;
