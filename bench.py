@@ -260,6 +260,21 @@ def dist_init():
     return world, rank, local, dist
 
 
+def max_over_ranks(dist, value):
+    """The slowest rank's time (the replicas run in step; the job ends with it)."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def replica_value(world, boxes_per_rank, ms):
+    """Whole-job boxes/s: every rank processes its own copy of the workload."""
+    return world * boxes_per_rank / (ms / 1e3)
+
+
 def run_reference(args, boxes, off, world, rank, dist):
     if rank != 0:
         return
@@ -385,10 +400,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t[0])
+    ms = max_over_ranks(dist, ms)
     clocks = clk.stop()
     ctx.sync()
     tile_ms_last, tile_launches, bin_, bout = ctx.profile_read()
@@ -459,7 +471,7 @@ def main():
     sort = None
     if rank == 0 and not args.no_sort:
         sort = sort_leg(n=args.sort_n, steps=3)
-    value = world * nbox / (ms / 1e3)
+    value = replica_value(world, nbox, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
