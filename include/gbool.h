@@ -288,6 +288,11 @@ void gb_serve_destroy(gb_server* s);
  * inner ring (P ~ P_2), ring_and1 (outer * P), ring_intersection
  * (outer * inner).  Asynchronous; capturable into a CUDA graph. */
 int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs);
+/* The same chain plus the deck's Klee union area of P per cell, written to
+ * d_area (device memory, one int64 per cell).  With a > 0 the area comes out
+ * of the erosion's complement (area(frame) - area(frame \ P)) with no extra
+ * pass; otherwise from a count-mode union of P.  Asynchronous, capturable. */
+int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, long long* d_area);
 /* The same deck through host buffers: boxes are copied in, the chain runs,
  * and per cell the six layer counts (counts[ncell*6], may be NULL) and the
  * union area of P (area[ncell], may be NULL) are copied out.

@@ -210,3 +210,37 @@ def test_op1_chain(ctx, oracle):
         assert int(ctx.area(P)[0]) == area
     finally:
         ctx.release(m)
+
+
+@pytest.mark.parametrize("amount", [1, 3, 0, -2])
+def test_op1_area_cells(ctx, oracle, amount):
+    """gb_op1_area: the chain's counts and the union area per cell (from the
+    erosion's complement when amount > 0), with empty cells among them."""
+    torch = pytest.importorskip("torch")
+    from gen import cells_layout
+    boxes, off = cells_layout(40, median=2000, seed=31 + amount)
+    # make two cells empty
+    keep = np.ones(len(boxes), bool)
+    for k in (3, 17):
+        keep[off[k]:off[k + 1]] = False
+    sizes = np.diff(off) * np.array([0 if k in (3, 17) else 1 for k in range(len(off) - 1)])
+    boxes = boxes[keep]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    m = ctx.mark()
+    try:
+        P = ctx.layer(boxes, off)
+        area_t = torch.full((len(off) - 1,), -7, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        outs = ctx.op1_area(P, amount, area_t.data_ptr())
+        ctx.sync()
+        area = area_t.cpu().numpy()
+        counts = np.stack([L.count()[1] for L in outs], axis=1)
+    finally:
+        ctx.release(m)
+    if amount == 1:
+        ec, ea = oracle.op1_cells(boxes, off)
+        assert np.array_equal(counts, ec)
+    else:
+        ea = np.array([oracle.union_area(boxes[off[k]:off[k + 1]]) for k in range(len(off) - 1)])
+    assert np.array_equal(area, ea)
+    assert area[3] == 0 and area[17] == 0

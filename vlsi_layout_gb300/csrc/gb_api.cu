@@ -597,7 +597,7 @@ extern "C" int gb_op_grow(gb_context* ctx, gb_layer* A, int32_t E, int32_t N, in
 }
 
 // SIZE(-t): R = P - ((F - P) (+) [-t,t]^2), F = cell bbox grown by t.
-gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t) {
+gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t, gb_layer** frame_out, gb_layer** comp_out) {
   GbCtx& c = ctx->c;
   const int g = 16;
   gb_layer* Pb = binned_of(ctx, P, g);
@@ -610,6 +610,8 @@ gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t) {
   k_fill_frame<<<(P->ncell + 255) / 256, 256, 0, c.stream>>>(Pb->d, F->d, P->ncell, t, c.st);
   gb_layer* Q = op_bool(ctx, GB_OP_NOT, F, Pb, 0);
   if (!Q) return nullptr;
+  if (frame_out) *frame_out = F;
+  if (comp_out) *comp_out = Q;
   gb_layer* D = op_grow(ctx, Q, t, t, t, t, false);
   if (!D) return nullptr;
   return op_bool(ctx, GB_OP_NOT, Pb, D, 0);

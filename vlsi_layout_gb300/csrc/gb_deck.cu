@@ -163,6 +163,53 @@ extern "C" int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs) 
   return GB_OK;
 }
 
+// Union area of P per cell from the erosion's complement: the frame F of a
+// cell contains P, so area(P) = area(F) - area(F \ P), and the tile kernel
+// has already summed area(F \ P) per cell.
+__global__ void k_area_from_frame(const DLayer* F, const DLayer* Q, long long* out, int ncell, DStatus* st) {
+  if (st->err) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncell; k += gridDim.x * blockDim.x) {
+    const int4 f = F->boxes[k];
+    out[k] = (long long)(f.z - f.x) * (long long)(f.w - f.y) - Q->cell_area[k];
+  }
+}
+
+__global__ void k_copy_area(const DLayer* A, long long* out, int ncell, DStatus* st) {
+  if (st->err) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncell; k += gridDim.x * blockDim.x) out[k] = A->cell_area[k];
+}
+
+// The OP1 chain plus the union area of P per cell into d_area (device, ncell
+// entries).  With a > 0 the area falls out of the erosion (no extra pass over
+// P); otherwise it is a count-mode union of P.  Asynchronous, capturable.
+extern "C" int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, long long* d_area) {
+  if (!ctx || !P || !outs || !d_area || P->dead) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  gb_layer* F = nullptr;
+  gb_layer* Q = nullptr;
+  gb_layer* p1 = a >= 0 ? op_grow(ctx, P, a, a, a, a, true) : op_erode(ctx, P, -a);
+  gb_layer* p2 = a > 0 ? op_erode(ctx, P, a, &F, &Q)
+                       : (a == 0 ? op_bool(ctx, GB_OP_MERGE, P, nullptr, 0) : op_grow(ctx, P, -a, -a, -a, -a, true));
+  if (!p1 || !p2) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  gb_layer* outer = op_bool(ctx, GB_OP_NOT, p1, P, 0);
+  gb_layer* inner = op_bool(ctx, GB_OP_NOT, P, p2, 0);
+  if (!outer || !inner) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  gb_layer* and1 = op_bool(ctx, GB_OP_AND, outer, P, 0);
+  gb_layer* inter = op_bool(ctx, GB_OP_AND, outer, inner, 0);
+  if (!and1 || !inter) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+  outs[0] = p1; outs[1] = p2; outs[2] = outer; outs[3] = inner; outs[4] = and1; outs[5] = inter;
+  const int nb = (P->ncell + 255) / 256;
+  if (F && Q) {
+    k_area_from_frame<<<nb, 256, 0, c.stream>>>(F->d, Q->d, d_area, P->ncell, c.st);
+  } else {
+    gb_layer* M = op_bool(ctx, GB_OP_MERGE, P, nullptr, 1);
+    if (!M) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
+    k_copy_area<<<nb, 256, 0, c.stream>>>(M->d, d_area, P->ncell, c.st);
+  }
+  ++c.launches;
+  return GB_OK;
+}
+
 __global__ void k_gather_counts(const DLayer* const* L, int nl, int ncell, long long* out,
                                 const DLayer* area_layer, long long* area_out, DStatus* st) {
   if (st->err) return;
@@ -189,14 +236,12 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
   cudaMalloc(&dl, 8 * sizeof(DLayer*));
   e = gb_run_retry(ctx, [&]() -> int {
     gb_layer* outs[6];
-    int r = gb_op1(ctx, P, a, outs);
+    int r = gb_op1_area(ctx, P, a, outs, darea);
     if (r) return r;
-    gb_layer* A = op_bool(ctx, GB_OP_MERGE, P, nullptr, 1);
-    if (!A) return GB_ERR_CAPACITY;
     DLayer* hl[6];
     for (int j = 0; j < 6; ++j) hl[j] = outs[j]->d;
     cudaMemcpyAsync(dl, hl, sizeof(hl), cudaMemcpyHostToDevice, c.stream);
-    k_gather_counts<<<(ncell + 255) / 256, 256, 0, c.stream>>>(dl, 6, ncell, dcounts, A->d, darea, c.st);
+    k_gather_counts<<<(ncell + 255) / 256, 256, 0, c.stream>>>(dl, 6, ncell, dcounts, nullptr, nullptr, c.st);
     return GB_OK;
   });
   std::vector<long long> hc((size_t)ncell * 6), ha(ncell);

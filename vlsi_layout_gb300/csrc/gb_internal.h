@@ -81,7 +81,11 @@ DLayer read_desc(gb_context* ctx, gb_layer* L);
 }
 gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode);
 gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge);
-gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t);
+// Erosion of P by the square [-t,t]^2.  frame_out / comp_out (optional)
+// receive the frame F (bbox of each cell grown by t, one box per cell) and
+// the complement Q = F \ P computed on the way.
+gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t, gb_layer** frame_out = nullptr,
+                   gb_layer** comp_out = nullptr);
 int sync_where(gb_context* ctx, int* where, long long* need);
 // Run a host-synchronous device sequence; on a capacity error enlarge the
 // failing resource (tile scratch, output slots) and run it again.

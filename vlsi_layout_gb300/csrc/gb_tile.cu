@@ -588,12 +588,21 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       __syncthreads();
       if (!s.err) {
-        int kx = w0 < W ? (int)s.xp[w0 >> 1] : 0, ky = w0 < W ? (int)s.yp[w0 >> 1] : 0;
-        for (int w = w0; w < w1; ++w) {
-          unsigned bits = s.xb[w];
-          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Xt[kx++] = (w << 5) + b; }
-          bits = s.yb[w];
-          while (bits) { const int b = __ffs(bits) - 1; bits &= bits - 1; s.Yt[ky++] = (w << 5) + b; }
+        // value tables, one word per thread in turn (set bits are spread, so
+        // the threads stay balanced); the rank of a word's first bit comes
+        // from the per-2-word prefix
+        int* xt = s.Xt;
+        int* yt = s.Yt;
+        for (int w = tid; w < W; w += TK_NT) {
+          unsigned bx = s.xb[w], by = s.yb[w];
+          if (bx) {
+            int k = (int)s.xp[w >> 1] + ((w & 1) ? __popc(s.xb[w - 1]) : 0);
+            while (bx) { const int b = __ffs(bx) - 1; bx &= bx - 1; xt[k++] = (w << 5) + b; }
+          }
+          if (by) {
+            int k = (int)s.yp[w >> 1] + ((w & 1) ? __popc(s.yb[w - 1]) : 0);
+            while (by) { const int b = __ffs(by) - 1; by &= by - 1; yt[k++] = (w << 5) + b; }
+          }
         }
       }
     }
@@ -735,28 +744,30 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       for (int sb = wid; sb < nsb; sb += TK_NW) {
         const int4 inf = s.sbinfo[sb];
         const PieceRec* src = s.sbrec[sb];
-        for (int j0 = lane; j0 < inf.y; j0 += TK_LD * 32) {
-          PieceRec r[TK_LD];
+        constexpr int RD = 4;
+        for (int j0 = lane; j0 < inf.y; j0 += RD * 32) {
+          PieceRec r[RD];
 #pragma unroll
-          for (int u = 0; u < TK_LD; ++u)
+          for (int u = 0; u < RD; ++u)
             if (j0 + u * 32 < inf.y) r[u] = src[j0 + u * 32];
 #pragma unroll
-          for (int u = 0; u < TK_LD; ++u)
+          for (int u = 0; u < RD; ++u)
             if (j0 + u * 32 < inf.y) PR[inf.x + j0 + u * 32] = r[u];
         }
       }
     if (xys) {
       const int* xt = s.Xt;
       const int* yt = s.Yt;
-      for (int i0 = tid; i0 < Nx + Ny; i0 += TK_LD * TK_NT) {
-        int v[TK_LD];
+      constexpr int VD = 8;
+      for (int i0 = tid; i0 < Nx + Ny; i0 += VD * TK_NT) {
+        int v[VD];
 #pragma unroll
-        for (int u = 0; u < TK_LD; ++u) {
+        for (int u = 0; u < VD; ++u) {
           const int i = i0 + u * TK_NT;
           v[u] = i < Nx ? xt[i] : i < Nx + Ny ? yt[i - Nx] : 0;
         }
 #pragma unroll
-        for (int u = 0; u < TK_LD; ++u)
+        for (int u = 0; u < VD; ++u)
           if (i0 + u * TK_NT < Nx + Ny) s.xyv[xyoff + i0 + u * TK_NT] = v[u];
       }
     }

@@ -82,6 +82,7 @@ def lib():
         "device_event_sort": (None, [P, i64]),
         "gb_op1": (ctypes.c_int, [P, P, i32, P]),
         "gb_op1_host": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P]),
+        "gb_op1_area": (ctypes.c_int, [P, P, i32, P, P]),
         "gb_graph_begin": (ctypes.c_int, [P]),
         "gb_graph_end": (ctypes.c_int, [P, pp]),
         "gb_graph_launch": (ctypes.c_int, [P, P]),
@@ -242,6 +243,13 @@ class Context:
         """OP1 deck on layer P; returns the six result layers."""
         outs = (ctypes.c_void_p * 6)()
         self._chk(lib().gb_op1(self.h, P.h, amount, outs))
+        return [Layer(self, ctypes.c_void_p(outs[i]), P.ncell) for i in range(6)]
+
+    def op1_area(self, P, amount, area_ptr):
+        """OP1 deck on layer P plus its union area per cell, written to the
+        device int64 array at area_ptr; returns the six result layers."""
+        outs = (ctypes.c_void_p * 6)()
+        self._chk(lib().gb_op1_area(self.h, P.h, amount, outs, area_ptr))
         return [Layer(self, ctypes.c_void_p(outs[i]), P.ncell) for i in range(6)]
 
     def op1_host(self, boxes_ptr, n, offsets, amount):
