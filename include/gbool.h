@@ -190,8 +190,8 @@ int gb_morton_sort(gb_context* ctx, c_box* boxes, long long n, int sort_boxes,
  * key bits, stable; the *_tmp buffers hold n entries.  The sorted pairs end
  * in d_keys / d_vals.  The pass count and keys per thread come from the
  * autotuner's table when it holds this device, bit width and size class,
- * else from the default (digits of at most 8 bits, an even pass count when
- * that costs no extra pass of bytes, tiles of 5120 keys).  n < 2^32.  Returns the number
+ * else from the default (digits of at most 7 bits, an even pass count when
+ * that costs no extra pass of bytes, tiles of 8192 keys).  n < 2^32.  Returns the number
  * of passes (>= 0) or minus a GB_ERR_* status.  Asynchronous on the context stream.
  * Replaces the Thrust radix sorts of gpu_morton.cu:149-187 and
  * event_sorter.cu:64-81 on device-resident data. */

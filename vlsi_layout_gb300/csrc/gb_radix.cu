@@ -8,7 +8,8 @@
 //  2. Each pass is one kernel: a CTA takes the next tile from an atomic
 //     counter (so tiles start in order) and pulls the tile's keys and values
 //     into shared memory with two bulk asynchronous copies completing on an
-//     mbarrier.  Warps rank the keys stably with per-bit ballots, the CTA
+//     mbarrier.  Warps rank the keys stably (peers by shared lane masks, or
+//     warp match and per-bit ballots for wide digits), the CTA
 //     publishes its per-digit counts, and obtains the exclusive prefix of all
 //     earlier tiles by a decoupled look-back over a status array.  Keys and
 //     values are then permuted in place in shared memory by digit and
@@ -150,10 +151,16 @@ __device__ __forceinline__ bool rs_mbar_wait(unsigned a, int limit) {
 }
 
 // ---------------------------------------------------------------- one pass
+// Radices up to RS_AO_RADIX find a key's peers through per-warp lane masks in
+// shared memory (one word per digit); larger ones by warp match / ballots.
+#define RS_AO_RADIX 128
+
 // Shared memory of a pass with NT threads, tile T = NT * IT keys and radix R:
 //   keys T*8 | vals T*4 | wh[NT/32][R] u16 | bstart[R] u32 | gpos[R] u32 | mbarrier, tile, scan scratch
+//   | lane masks [NT/32][R] u32 when R <= RS_AO_RADIX
 __host__ __device__ constexpr size_t rs_smem_bytes(int nt, int it, int radix) {
-  return (size_t)nt * it * 12 + (size_t)(nt / 32) * radix * 2 + (size_t)radix * 8 + 16 + 33 * 8;
+  return (size_t)nt * it * 12 + (size_t)(nt / 32) * radix * 2 + (size_t)radix * 8 + 16 + 33 * 8 +
+         (radix <= RS_AO_RADIX ? (size_t)(nt / 32) * radix * 4 : 0);
 }
 
 // The digit [shift, shift + dbits) of a key, taken from its two 32-bit words
@@ -173,7 +180,8 @@ struct RsDigit {
 // look-back and write-out.  FULL: the tile holds TILE keys (no bounds tests).
 template <int NT, int IT, int MAXB, bool FULL>
 __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, unsigned short* wh, unsigned* bstart,
-                                        unsigned* gpos, long long* tmp, const RsDigit& digit, int radix, int cnt,
+                                        unsigned* gpos, long long* tmp, unsigned* mbuf, const RsDigit& digit,
+                                        int radix, int cnt,
                                         long long tile, long long ntile, const unsigned* __restrict__ gofs,
                                         unsigned long long* status, unsigned long long epoch, DStatus* st,
                                         int spin_limit, unsigned long long* __restrict__ kout,
@@ -182,9 +190,9 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
   constexpr int NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   // ---- rank: warp w owns keys [w*32*IT, (w+1)*32*IT) in order.  Peers with
-  // the same digit are found by a warp match (every third item) or one
-  // ballot per digit bit (the others), so the match unit and the integer pipe
-  // share the work; the lowest peer adds the group to the warp's counter (two 16-bit counters share a 32-bit
+  // the same digit are found through shared lane masks (radix <= RS_AO_RADIX)
+  // or by a warp match (every third item) and one ballot per digit bit (the
+  // others), so the match unit and the integer pipe share the work; the lowest peer adds the group to the warp's counter (two 16-bit counters share a 32-bit
   // word; a count never exceeds 32*IT, so no carry crosses halves) and
   // broadcasts the old value.  Keys stay in registers; ranks are packed two
   // to a register.
@@ -201,7 +209,22 @@ __device__ __forceinline__ void rs_tile(unsigned long long* sk, unsigned* sv, un
     kk[it] = ok ? sk[idx] : 0ull;
     const unsigned d = digit(kk[it]);
     unsigned peers;
-    if (it % 3 == 1) {
+    if (radix <= RS_AO_RADIX) {
+      // lane masks: each lane ORs its bit into its warp's word for its digit
+      // and reads the word back (shared-memory pipe, no votes); the peers
+      // then clear it for the next item
+      unsigned* mm = mbuf + wid * radix;
+      if (ok) atomicOr(&mm[d], 1u << lane);
+      __syncwarp();
+      peers = ok ? mm[d] : 0u;
+      if (!FULL) {
+        const unsigned vm = __ballot_sync(0xffffffffu, ok);
+        if (!ok) peers = ~vm;
+      }
+      __syncwarp();
+      if (ok) mm[d] = 0u;
+      __syncwarp();
+    } else if (it % 3 == 1) {
       // every third item: warp match (its own pipe), invalid lanes carry an out-of-range digit
       peers = __match_any_sync(0xffffffffu, ok ? d : 0xFFFFFFFFu);
     } else {
@@ -379,6 +402,7 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
   unsigned long long* mbar = reinterpret_cast<unsigned long long*>(gpos + radix);
   long long* stile = reinterpret_cast<long long*>(mbar + 1);
   long long* tmp = stile + 1;  // [33]
+  unsigned* mbuf = reinterpret_cast<unsigned*>(tmp + 33);  // [NW][radix] lane masks (radix <= RS_AO_RADIX)
   const int tid = threadIdx.x;
   const long long ntile = (n + TILE - 1) / TILE;
   const unsigned mb = rs_smem(mbar);
@@ -398,6 +422,8 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
     }
   }
   for (int i = tid; i < NW * radix / 2; i += NT) reinterpret_cast<unsigned*>(wh)[i] = 0u;
+  if (radix <= RS_AO_RADIX)
+    for (int i = tid; i < NW * radix; i += NT) mbuf[i] = 0u;
   __syncthreads();
   const long long tile = *stile;
   if (tile >= ntile) return;
@@ -423,10 +449,10 @@ k_rs_pass(const unsigned long long* __restrict__ kin, const unsigned* __restrict
   }
 
   if (cnt == TILE)
-    rs_tile<NT, IT, MAXB, true>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+    rs_tile<NT, IT, MAXB, true>(sk, sv, wh, bstart, gpos, tmp, mbuf, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
                             spin_limit, kout, vout);
   else
-    rs_tile<NT, IT, MAXB, false>(sk, sv, wh, bstart, gpos, tmp, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
+    rs_tile<NT, IT, MAXB, false>(sk, sv, wh, bstart, gpos, tmp, mbuf, digit, radix, cnt, tile, ntile, gofs, status, epoch, st,
                              spin_limit, kout, vout);
 }
 
@@ -513,11 +539,11 @@ void gb_radix_free(GbCtx& c) {
 }
 
 // Default configuration for a sort of `bits` significant bits: the fewest
-// passes with digits of at most 8 bits, one more when that makes the count
-// even (it moves as many bytes as the final copy it saves, in narrower and
-// better-coalesced digit runs), tiles of 8192 keys.
+// passes with digits of at most 7 bits (radix <= RS_AO_RADIX ranks through
+// shared lane masks), one more when that makes the count even (it moves as
+// many bytes as the final copy it saves), tiles of 8192 keys.
 void gb_radix_default(int bits, int* passes, int* tile) {
-  int p = (bits + 7) / 8;
+  int p = (bits + 6) / 7;
   if ((p & 1) && p + 1 <= bits) ++p;
   *passes = std::max(1, p);
   *tile = 8192;
@@ -567,7 +593,10 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
     cudaMemsetAsync(S->status, 0, want * 8, c.stream);
     S->status_words = want;
   }
-  const size_t smem = rs_smem_bytes(K->nt, K->it, maxradix);
+  // passes of different digit widths lay shared memory out differently (the
+  // lane masks exist only for radix <= RS_AO_RADIX): size for the largest
+  size_t smem = 0;
+  for (int p = 0; p < passes; ++p) smem = std::max(smem, rs_smem_bytes(K->nt, K->it, 1 << plan.bits[p]));
   for (int i = 0; i < 4; ++i) {
     cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute((const void*)K->fn[i], cudaFuncAttributePreferredSharedMemoryCarveout, 100);
