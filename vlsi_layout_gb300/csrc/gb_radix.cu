@@ -3,8 +3,9 @@
 // tracker events (event_sorter.cu:48-81) and canonical strip order.
 //
 //  1. One read of the keys builds the digit histograms of every pass
-//     (per-CTA shared-memory counters, merged with global atomics; a digit
-//     that is the same across a warp is counted with one atomic).
+//     (one CTA per SM with shared-memory counters, merged with global
+//     atomics; two adjacent narrow passes share a joint table, so a shared
+//     atomic counts a key for both).
 //  2. Each pass is one kernel: a CTA takes the next tile from an atomic
 //     counter (so tiles start in order) and pulls the tile's keys and values
 //     into shared memory with two bulk asynchronous copies completing on an
@@ -48,55 +49,89 @@ struct RsPlan {
 };
 
 // ---------------------------------------------------------------- histogram
-template <bool V2>
-__global__ void __launch_bounds__(256)
-k_rs_hist(const unsigned long long* __restrict__ keys, long long n, RsPlan plan, unsigned* __restrict__ ghist) {
-  __shared__ unsigned h[RS_HIST_SLOTS];
-  const int tot_slots = plan.off[plan.np - 1] + (1 << plan.bits[plan.np - 1]);
-  for (int i = threadIdx.x; i < tot_slots; i += blockDim.x) h[i] = 0;
+// Counters of adjacent passes whose digits together are at most
+// RS_JOINT_BITS wide are kept as one joint table indexed by both digits (a
+// 7-bit and a 7-bit digit: 16384 counters), so one shared atomic counts a key
+// for two passes; each pass's counts are the table's row or column sums.
+#define RS_JOINT_BITS 14
+#define RS_HIST_WORDS (48 * 1024)  // shared counters of one histogram CTA (192 KB)
+#define RS_HIST_KPT 4              // keys per thread per step
+
+struct RsHistPlan {
+  int ng;                // counter groups
+  int words;             // shared counters in all groups
+  int gshift[RS_MAXPASS];  // shift of the group's low digit
+  int gbits[RS_MAXPASS];   // width of the group's (joint) index
+  int goff[RS_MAXPASS];    // offset of the group's counters in shared memory
+  int gp[RS_MAXPASS];      // first pass of the group
+  int gn[RS_MAXPASS];      // passes in the group: 1 or 2
+};
+
+template <bool VEC>
+__global__ void __launch_bounds__(1024, 1)
+k_rs_hist(const unsigned long long* __restrict__ keys, long long n, RsPlan plan, RsHistPlan hp,
+          unsigned* __restrict__ ghist) {
+  extern __shared__ unsigned hj[];
+  const int ng = hp.ng;
+  for (int i = threadIdx.x; i < hp.words; i += blockDim.x) hj[i] = 0;
+  __syncthreads();
+  const long long nq = n / RS_HIST_KPT;
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += step) {
+    unsigned long long k[RS_HIST_KPT];
+    if (VEC) {
+      const ulonglong2* q = reinterpret_cast<const ulonglong2*>(keys) + (RS_HIST_KPT / 2) * i;
+#pragma unroll
+      for (int j = 0; j < RS_HIST_KPT / 2; ++j) {
+        const ulonglong2 a = q[j];
+        k[2 * j] = a.x;
+        k[2 * j + 1] = a.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < RS_HIST_KPT; ++j) k[j] = keys[RS_HIST_KPT * i + j];
+    }
+#pragma unroll
+    for (int g = 0; g < RS_MAXPASS; ++g) {
+      if (g >= ng) break;
+      const int sh = hp.gshift[g];
+      const unsigned m = (1u << hp.gbits[g]) - 1u;
+      unsigned* t = hj + hp.goff[g];
+#pragma unroll
+      for (int j = 0; j < RS_HIST_KPT; ++j) atomicAdd(&t[(unsigned)(k[j] >> sh) & m], 1u);
+    }
+  }
+  const long long r0 = nq * RS_HIST_KPT;
+  if (blockIdx.x == 0 && threadIdx.x < n - r0) {
+    const unsigned long long kk = keys[r0 + threadIdx.x];
+    for (int g = 0; g < ng; ++g)
+      atomicAdd(&hj[hp.goff[g] + ((unsigned)(kk >> hp.gshift[g]) & ((1u << hp.gbits[g]) - 1u))], 1u);
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const long long step = (long long)gridDim.x * blockDim.x;
-  // items: pairs of keys (V2) or single keys
-  const long long nit = V2 ? (n >> 1) : n;
-  for (long long wb = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); wb < nit; wb += step) {
-    const long long i = wb + lane;
-    const bool ok = i < nit;
-    const unsigned okm = __ballot_sync(0xffffffffu, ok);
-    unsigned long long k0 = 0, k1 = 0;
-    if (ok) {
-      if (V2) {
-        const ulonglong2 v = reinterpret_cast<const ulonglong2*>(keys)[i];
-        k0 = v.x;
-        k1 = v.y;
-      } else {
-        k0 = keys[i];
-        k1 = k0;
+  for (int g = 0; g < ng; ++g) {
+    const unsigned* t = hj + hp.goff[g];
+    const int p = hp.gp[g];
+    if (hp.gn[g] == 1) {
+      for (int d = threadIdx.x; d < (1 << hp.gbits[g]); d += blockDim.x) {
+        const unsigned v = t[d];
+        if (v) atomicAdd(&ghist[plan.off[p] + d], v);
       }
+      continue;
     }
-    const int first = __ffs(okm) - 1;
-    for (int p = 0; p < plan.np; ++p) {
-      const unsigned m = (1u << plan.bits[p]) - 1u;
-      const unsigned d0 = (unsigned)(k0 >> plan.shift[p]) & m;
-      const unsigned d1 = (unsigned)(k1 >> plan.shift[p]) & m;
-      const unsigned dl = __shfl_sync(0xffffffffu, d0, first);
-      if (__all_sync(0xffffffffu, !ok || (d0 == dl && d1 == dl))) {
-        if (lane == first) atomicAdd(&h[plan.off[p] + dl], (unsigned)__popc(okm) * (V2 ? 2u : 1u));
-      } else if (ok) {
-        atomicAdd(&h[plan.off[p] + d0], 1u);
-        if (V2) atomicAdd(&h[plan.off[p] + d1], 1u);
-      }
+    // joint index = low digit | high digit << bl
+    const int bl = plan.bits[p], rl = 1 << bl, rh = 1 << plan.bits[p + 1];
+    for (int d = threadIdx.x; d < rl; d += blockDim.x) {  // low pass: column sums
+      unsigned v = 0;
+      for (int e = 0; e < rh; ++e) v += t[(e << bl) | d];
+      if (v) atomicAdd(&ghist[plan.off[p] + d], v);
     }
-  }
-  if (V2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    const unsigned long long k = keys[n - 1];
-    for (int p = 0; p < plan.np; ++p)
-      atomicAdd(&h[plan.off[p] + ((unsigned)(k >> plan.shift[p]) & ((1u << plan.bits[p]) - 1u))], 1u);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < tot_slots; i += blockDim.x) {
-    const unsigned v = h[i];
-    if (v) atomicAdd(&ghist[i], v);
+    for (int e = threadIdx.x >> 5; e < rh; e += blockDim.x >> 5) {  // high pass: row sums, a warp per row
+      unsigned v = 0;
+      for (int d = lane; d < rl; d += 32) v += t[(e << bl) | d];
+      v = __reduce_add_sync(0xffffffffu, v);
+      if (lane == 0 && v) atomicAdd(&ghist[plan.off[p + 1] + e], v);
+    }
   }
 }
 
@@ -516,6 +551,36 @@ void make_plan(int bits, int passes, RsPlan& p) {
   }
 }
 
+// Groups the passes' counters for k_rs_hist: each pass alone, then adjacent
+// pairs joined left to right while the joint index stays within
+// RS_JOINT_BITS and all counters fit in RS_HIST_WORDS.
+void make_hist_plan(const RsPlan& p, RsHistPlan& h) {
+  int words = 0;
+  for (int i = 0; i < p.np; ++i) words += 1 << p.bits[i];
+  h.ng = 0;
+  int off = 0;
+  for (int i = 0; i < p.np;) {
+    const int g = h.ng++;
+    h.gshift[g] = p.shift[i];
+    h.gp[g] = i;
+    const int jb = i + 1 < p.np ? p.bits[i] + p.bits[i + 1] : 99;
+    const int extra = jb <= RS_JOINT_BITS ? (1 << jb) - (1 << p.bits[i]) - (1 << p.bits[i + 1]) : 0;
+    if (jb <= RS_JOINT_BITS && words + extra <= RS_HIST_WORDS) {
+      words += extra;
+      h.gbits[g] = jb;
+      h.gn[g] = 2;
+      i += 2;
+    } else {
+      h.gbits[g] = p.bits[i];
+      h.gn[g] = 1;
+      i += 1;
+    }
+    h.goff[g] = off;
+    off += 1 << h.gbits[g];
+  }
+  h.words = off;
+}
+
 // process-wide table of tuned configurations: (device, bits, log2 n) -> (passes, tile keys)
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned;
@@ -603,10 +668,19 @@ int gb_radix_sort_pairs(GbCtx& c, unsigned long long* keys, unsigned* vals, long
   }
   const bool al = !(((uintptr_t)keys | (uintptr_t)vals | (uintptr_t)keys_tmp | (uintptr_t)vals_tmp) & 15u);
   k_rs_zero<<<1, 1024, 0, c.stream>>>(S->ghist, RS_HIST_SLOTS, S->ctrs, RS_MAXPASS);
-  if (!((uintptr_t)keys & 15u))
-    k_rs_hist<true><<<c.nsm * 4, 256, 0, c.stream>>>(keys, n, plan, S->ghist);
-  else
-    k_rs_hist<false><<<c.nsm * 4, 256, 0, c.stream>>>(keys, n, plan, S->ghist);
+  RsHistPlan hplan;
+  make_hist_plan(plan, hplan);
+  {
+    const size_t hsm = (size_t)hplan.words * sizeof(unsigned);
+    const long long want_blocks = (n / RS_HIST_KPT + 1023) / 1024;
+    const unsigned hb = (unsigned)std::max(1ll, std::min<long long>(c.nsm, want_blocks));
+    const void* hf = !((uintptr_t)keys & 15u) ? (const void*)k_rs_hist<true> : (const void*)k_rs_hist<false>;
+    cudaFuncSetAttribute(hf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+    if (!((uintptr_t)keys & 15u))
+      k_rs_hist<true><<<hb, 1024, hsm, c.stream>>>(keys, n, plan, hplan, S->ghist);
+    else
+      k_rs_hist<false><<<hb, 1024, hsm, c.stream>>>(keys, n, plan, hplan, S->ghist);
+  }
   k_rs_hist_scan<<<passes, 1024, 0, c.stream>>>(S->ghist, plan);
   c.launches += 3;
   unsigned long long* ka = keys;
