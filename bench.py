@@ -338,12 +338,13 @@ def main():
     ap.add_argument("--sort-only", action="store_true")
     ap.add_argument("--sort-n", type=int, default=200_000_000)
     ap.add_argument("--no-sort", action="store_true")
+    ap.add_argument("--sort-no-tune", action="store_true", help="time the default sort plan only")
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
     if args.sort_only:
         import torch
         torch.cuda.set_device(local)
-        print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps)}), flush=True)
+        print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps, tune=not args.sort_no_tune)}), flush=True)
         return
     if args.serve_only:
         import torch
