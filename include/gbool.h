@@ -43,6 +43,7 @@ extern "C" {
 #define GB_ERR_CUDA 5
 #define GB_ERR_ARG 6
 #define GB_ERR_INTERNAL 7
+#define GB_ERR_CORRUPT 8       /* a SNAP stream or file is malformed (codec desync, bad Snappy element) */
 
 /* ---- Boolean opcodes (the reference's control parameter, boost_polygon_api.cpp:116-137) */
 #define GB_OP_XOR 0
@@ -300,6 +301,47 @@ int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, long l
 int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
                 const long long* cell_offsets, int ncell, int32_t a, long long* counts,
                 long long* area, int* assert_failures);
+
+/* ---- SNAP layer streams (box_codec.f90, serialization.f90, snappy_api.cpp)
+ * A stream is the layer's boxes cut into chunks of 65536; each chunk is the
+ * box codec's byte stream (infobyte, zigzag varint anchor deltas, width /
+ * height dictionaries by first appearance: CompressBoxesUsingCodec,
+ * box_codec.f90:616-698), compressed with method 1 (Snappy raw format, as
+ * snappy_compress_buffer, box_codec.f90:732-734) or stored as is with
+ * method 0.  ZLIB (2) and ZSTD (3) are refused with GB_ERR_ARG.
+ * chunk_meta holds three int64 per chunk, as the chunk header of a .snap
+ * file: num_boxes, raw_byte_size, compressed_size.  Synchronous. */
+/* Bound of the device bytes a stream of n boxes can take. */
+int gb_snap_max_bytes(long long n, long long* bytes);
+/* CompressBoxesToStream (box_codec.f90:675-760) on n device boxes (16-byte
+ * aligned).  The chunks' data go back to back into d_out (cap bytes;
+ * GB_ERR_CAPACITY when short); chunk_meta (host, 3 * ceil(n / 65536)) and
+ * *total (bytes used) are filled. */
+int gb_compress_boxes_to_stream(gb_context* ctx, const c_box* d_boxes, long long n, int method,
+                                unsigned char* d_out, long long cap, long long* chunk_meta, long long* total);
+/* DecompressStreamToBoxes (box_codec.f90:765-880): num_chunks chunks whose
+ * data lie back to back at d_data (device), described by chunk_meta (host),
+ * into d_boxes (device, sum of num_boxes entries).  A malformed stream (codec
+ * desync, bad Snappy element, sizes that disagree with the header) gives
+ * GB_ERR_CORRUPT; the reference stops there. */
+int gb_decompress_stream_to_boxes(gb_context* ctx, const unsigned char* d_data, const long long* chunk_meta,
+                                  long long num_chunks, int method, c_box* d_boxes);
+/* SaveLayerToSnap + SaveCompressedStreamToDisk (diskdesign_impl.f90:59-82,
+ * serialization.f90:15-50): the .snap file of n device boxes.  pnum (host,
+ * n int64, may be NULL) is stored after the header and sets the PNUM bit (4)
+ * of layer_properties; without it the bit is cleared; the R-tree bit (8) is
+ * never saved. */
+int gb_save_layer_to_snap(gb_context* ctx, const char* path, const c_box* d_boxes, long long n, int method,
+                          int layer_properties, const long long* pnum);
+/* Header of a .snap file (an empty file is an empty layer). */
+int gb_snap_file_info(const char* path, long long* total_boxes, long long* num_chunks, int* method,
+                      int* layer_properties);
+/* RestoreSnapToLayer (diskdesign_impl.f90:84-113): the file's boxes into
+ * d_boxes (device, cap entries; *n receives the count, GB_ERR_CAPACITY when
+ * cap is short) and, when pnum is not NULL and the file holds one, its PNUM
+ * table (host, n int64). */
+int gb_restore_snap_to_layer(gb_context* ctx, const char* path, c_box* d_boxes, long long cap, long long* n,
+                             long long* pnum);
 
 /* CUDA-graph capture of an operator chain on the context stream.  Every
  * replay restarts the work arena at the offset it had at gb_graph_begin. */

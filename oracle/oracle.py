@@ -24,8 +24,7 @@ _lib = None
 
 def build(force=False):
     """Compile the oracle (and the reference CPU sort helpers when mounted)."""
-    if force or not os.path.exists(_LIB):
-        subprocess.check_call(["make", "-s", "-C", _HERE, "_build/libgbo_oracle.so"])
+    subprocess.check_call(["make", "-s", "-C", _HERE, "_build/libgbo_oracle.so"] + (["-B"] if force else []))
     subprocess.call(["make", "-s", "-C", _HERE, "ref"], stdout=subprocess.DEVNULL)
 
 
@@ -61,6 +60,18 @@ def lib():
         L.orc_op1.restype = None
         L.orc_op1_cells.argtypes = [P, P, i64, i32, ctypes.c_int, P, P]
         L.orc_op1_cells.restype = None
+        L.orc_codec_encode.argtypes = [P, i64, P]
+        L.orc_codec_encode.restype = i64
+        L.orc_codec_decode.argtypes = [P, i64, i64, P]
+        L.orc_codec_decode.restype = i64
+        L.orc_snappy_max_length.argtypes = [i64]
+        L.orc_snappy_max_length.restype = i64
+        L.orc_snappy_compress.argtypes = [P, i64, P]
+        L.orc_snappy_compress.restype = i64
+        L.orc_snappy_uncompressed_length.argtypes = [P, i64]
+        L.orc_snappy_uncompressed_length.restype = i64
+        L.orc_snappy_decompress.argtypes = [P, i64, P, i64]
+        L.orc_snappy_decompress.restype = i64
         L.orc_free.argtypes = [P]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -240,3 +251,115 @@ def ref_sort_lib():
     L.thrust_sort_boxes_indirect.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
     L.cpp_std_sort_trackers.argtypes = [ctypes.c_void_p, ctypes.c_int64]
     return L
+
+
+# ---------------------------------------------------------------- SNAP codec
+# box_codec.f90 (BoxCodecModule) and serialization.f90; see gbo_snap.cpp.
+BOXES_PER_CHUNK = 65536          # box_codec.f90:227
+CODEC_VERSION = 1                # commonmodule.f90:22
+METHOD_NONE, METHOD_SNAPPY = 0, 1  # box_codec.f90:228-233
+LAYER_STATE_PNUM = 4             # design.f90:41
+
+
+def _u8(b):
+    return np.frombuffer(bytes(b), np.uint8) if not isinstance(b, np.ndarray) else np.ascontiguousarray(b, np.uint8)
+
+
+def codec_encode_chunk(A):
+    """CompressBoxesUsingCodec on one chunk: the raw codec bytes."""
+    A = _arr(A)
+    out = np.zeros(32 * len(A) + 1, np.uint8)
+    k = lib().orc_codec_encode(A.ctypes.data, len(A), out.ctypes.data)
+    return out[:k].tobytes()
+
+
+def codec_decode_chunk(raw, n):
+    """DecompressBoxesUsingCodec: n boxes from raw codec bytes (ValueError on desync)."""
+    r = _u8(raw)
+    out = np.zeros((n, 4), np.int32)
+    k = lib().orc_codec_decode(r.ctypes.data, len(r), n, out.ctypes.data)
+    if k != 0:
+        raise ValueError("codec stream desync at record %d" % (-k - 1))
+    return out
+
+
+def snappy_compress(raw):
+    r = _u8(raw)
+    out = np.zeros(lib().orc_snappy_max_length(len(r)), np.uint8)
+    k = lib().orc_snappy_compress(r.ctypes.data, len(r), out.ctypes.data)
+    return out[:k].tobytes()
+
+
+def snappy_decompress(data):
+    d = _u8(data)
+    n = lib().orc_snappy_uncompressed_length(d.ctypes.data, len(d))
+    if n < 0:
+        raise ValueError("bad snappy preamble")
+    out = np.zeros(max(n, 1), np.uint8)
+    k = lib().orc_snappy_decompress(d.ctypes.data, len(d), out.ctypes.data, n)
+    if k != n:
+        raise ValueError("malformed snappy stream")
+    return out[:n].tobytes()
+
+
+def stream_encode(A, method=METHOD_SNAPPY):
+    """CompressBoxesToStream (box_codec.f90:675-760): per chunk
+    (num_boxes, raw_byte_size, compressed_size, data)."""
+    A = _arr(A)
+    chunks = []
+    for c0 in range(0, len(A), BOXES_PER_CHUNK):
+        part = A[c0:c0 + BOXES_PER_CHUNK]
+        raw = codec_encode_chunk(part)
+        data = snappy_compress(raw) if method == METHOD_SNAPPY else raw
+        chunks.append((len(part), len(raw), len(data), data))
+    return chunks
+
+
+def stream_decode(chunks, method=METHOD_SNAPPY):
+    """DecompressStreamToBoxes (box_codec.f90:765-880)."""
+    parts = []
+    for nb, raw_n, comp_n, data in chunks:
+        raw = snappy_decompress(data) if method == METHOD_SNAPPY else bytes(data)
+        if len(raw) != raw_n:
+            raise ValueError("raw size differs from the chunk header")
+        parts.append(codec_decode_chunk(raw, nb))
+    return np.concatenate(parts) if parts else np.zeros((0, 4), np.int32)
+
+
+def snap_file_bytes(A, method=METHOD_SNAPPY, layer_properties=0, pnum=None):
+    """SaveCompressedStreamToDisk (serialization.f90:15-50): int32 version,
+    int32 layer properties, int64 total boxes, int64 chunks, int32 method,
+    [int64 PNUM table], then per chunk three int64 and the data, then the
+    int64 table of the chunks' 1-based file positions and, last, the int64
+    1-based position of that table."""
+    import struct
+    chunks = stream_encode(A, method)
+    out = bytearray(struct.pack("<iiqqi", CODEC_VERSION, layer_properties, len(_arr(A)), len(chunks), method))
+    if pnum is not None:
+        out += np.ascontiguousarray(pnum, np.int64).tobytes()
+    offs = []
+    for nb, raw_n, comp_n, data in chunks:
+        offs.append(len(out) + 1)
+        out += struct.pack("<qqq", nb, raw_n, comp_n) + bytes(data)
+    table = len(out) + 1
+    out += np.array(offs, np.int64).tobytes() + struct.pack("<q", table)
+    return bytes(out)
+
+
+def snap_file_parse(buf):
+    """RestoreCompressedStreamFromDisk (serialization.f90:56-130):
+    (layer_properties, method, chunks, pnum or None)."""
+    import struct
+    ver, props, total, nch, method = struct.unpack_from("<iiqqi", buf, 0)
+    p = 28
+    pnum = None
+    if props & LAYER_STATE_PNUM:
+        pnum = np.frombuffer(buf, np.int64, total, p).copy()
+        p += 8 * total
+    chunks = []
+    for _ in range(nch):
+        nb, raw_n, comp_n = struct.unpack_from("<qqq", buf, p)
+        p += 24
+        chunks.append((nb, raw_n, comp_n, bytes(buf[p:p + comp_n])))
+        p += comp_n
+    return props, method, chunks, pnum

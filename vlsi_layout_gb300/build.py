@@ -15,7 +15,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbool.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gb_bin.cu", "gb_tile.cu", "gb_uf.cu", "gb_radix.cu", "gb_api.cu", "gb_deck.cu",
-           "gb_deckrun.cu", "gb_serve.cu"]
+           "gb_deckrun.cu", "gb_serve.cu", "gb_snap.cu"]
 
 
 def _nvcc():

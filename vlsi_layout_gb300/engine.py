@@ -18,11 +18,15 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libgbool.so")
 
 GB_OK, GB_ERR_CAPACITY, GB_ERR_INVALID_BOX, GB_ERR_OOM, GB_ERR_TIMEOUT, GB_ERR_CUDA, GB_ERR_ARG, \
-    GB_ERR_INTERNAL = range(8)
+    GB_ERR_INTERNAL, GB_ERR_CORRUPT = range(9)
 XOR, OR, AND, NOT, MERGE, SIZE = range(6)
 OVERLAP = 7  # single-layer AND: area covered by at least two boxes of A
 
-_ERRNAMES = {1: "CAPACITY", 2: "INVALID_BOX", 3: "OOM", 4: "TIMEOUT", 5: "CUDA", 6: "ARG", 7: "INTERNAL"}
+_ERRNAMES = {1: "CAPACITY", 2: "INVALID_BOX", 3: "OOM", 4: "TIMEOUT", 5: "CUDA", 6: "ARG", 7: "INTERNAL",
+             8: "CORRUPT"}
+# SNAP streams (box_codec.f90 / serialization.f90)
+SNAP_BOXES_PER_CHUNK = 65536
+COMPRESSION_METHOD_NONE, COMPRESSION_METHOD_SNAPPY = 0, 1
 
 
 class GBError(RuntimeError):
@@ -107,6 +111,12 @@ def lib():
         "gb_serve_result_boxes": (ctypes.c_int, [P, ctypes.c_int, P, u64, P]),
         "gb_serve_destroy": (None, [P]),
         "gb_bool_tile_noalloc": (ctypes.c_int, [ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, i64, P, P, P]),
+        "gb_snap_max_bytes": (ctypes.c_int, [i64, P]),
+        "gb_compress_boxes_to_stream": (ctypes.c_int, [P, P, i64, ctypes.c_int, P, i64, P, P]),
+        "gb_decompress_stream_to_boxes": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P]),
+        "gb_save_layer_to_snap": (ctypes.c_int, [P, ctypes.c_char_p, P, i64, ctypes.c_int, ctypes.c_int, P]),
+        "gb_snap_file_info": (ctypes.c_int, [ctypes.c_char_p, P, P, P, P]),
+        "gb_restore_snap_to_layer": (ctypes.c_int, [P, ctypes.c_char_p, P, i64, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -331,6 +341,69 @@ class Context:
             self._chk(-r)
         return r
 
+    # ---- SNAP streams: box codec + Snappy per 65536-box chunk, .snap files
+    def compress_boxes_to_stream(self, boxes, method=COMPRESSION_METHOD_SNAPPY):
+        """CompressBoxesToStream on the device.  boxes: numpy (n, 4) int32 or
+        a CUDA int32 tensor.  Returns [(num_boxes, raw_byte_size,
+        compressed_size, data bytes)] per chunk."""
+        import torch
+        d = _device_boxes(boxes)
+        n = d.shape[0]
+        cap = ctypes.c_int64()
+        self._chk(lib().gb_snap_max_bytes(n, ctypes.byref(cap)))
+        out = torch.empty(max(cap.value, 16), dtype=torch.uint8, device=d.device)
+        nch = (n + SNAP_BOXES_PER_CHUNK - 1) // SNAP_BOXES_PER_CHUNK
+        meta = np.zeros(3 * max(nch, 1), np.int64)
+        tot = ctypes.c_int64()
+        torch.cuda.synchronize(d.device)
+        self._chk(lib().gb_compress_boxes_to_stream(self.h, d.data_ptr(), n, method, out.data_ptr(), cap.value,
+                                                    meta.ctypes.data, ctypes.byref(tot)))
+        data = out[:tot.value].cpu().numpy().tobytes()
+        chunks, at = [], 0
+        for i in range(nch):
+            nb, rn, cn = (int(v) for v in meta[3 * i:3 * i + 3])
+            chunks.append((nb, rn, cn, data[at:at + cn]))
+            at += cn
+        return chunks
+
+    def decompress_stream_to_boxes(self, chunks, method=COMPRESSION_METHOD_SNAPPY, as_tensor=False):
+        """DecompressStreamToBoxes on the device: chunks as returned by
+        compress_boxes_to_stream (or read from a .snap file)."""
+        import torch
+        n = sum(c[0] for c in chunks)
+        meta = np.array([v for c in chunks for v in c[:3]] or [0], np.int64)
+        data = b"".join(bytes(c[3]) for c in chunks)
+        dd = torch.frombuffer(bytearray(data) or bytearray(16), dtype=torch.uint8).cuda()
+        out = torch.empty((max(n, 1), 4), dtype=torch.int32, device=dd.device)
+        torch.cuda.synchronize(dd.device)
+        self._chk(lib().gb_decompress_stream_to_boxes(self.h, dd.data_ptr(), meta.ctypes.data, len(chunks), method,
+                                                      out.data_ptr()))
+        out = out[:n]
+        return out if as_tensor else out.cpu().numpy()
+
+    def save_layer_to_snap(self, path, boxes, method=COMPRESSION_METHOD_SNAPPY, layer_properties=0, pnum=None):
+        """SaveLayerToSnap / SaveCompressedStreamToDisk: write boxes (numpy or
+        CUDA tensor) as a .snap file; pnum (int64 per box) is stored when given."""
+        import torch
+        d = _device_boxes(boxes)
+        pn = None if pnum is None else np.ascontiguousarray(pnum, np.int64)
+        torch.cuda.synchronize(d.device)
+        self._chk(lib().gb_save_layer_to_snap(self.h, os.fsencode(path), d.data_ptr(), d.shape[0], method,
+                                              layer_properties, None if pn is None else pn.ctypes.data))
+
+    def restore_snap_to_layer(self, path, as_tensor=False):
+        """RestoreSnapToLayer: (boxes, layer_properties, method, pnum or None)."""
+        import torch
+        n, nch, meth, props = snap_file_info(path)
+        out = torch.empty((max(n, 1), 4), dtype=torch.int32, device="cuda")
+        pn = np.zeros(max(n, 1), np.int64) if props & 4 else None
+        got = ctypes.c_int64()
+        torch.cuda.synchronize()
+        self._chk(lib().gb_restore_snap_to_layer(self.h, os.fsencode(path), out.data_ptr(), n, ctypes.byref(got),
+                                                 None if pn is None else pn.ctypes.data))
+        out = out[:n]
+        return (out if as_tensor else out.cpu().numpy()), props, meth, (pn[:n] if pn is not None else None)
+
     def radix_autotune(self, keys_ptr, vals_ptr, n, bits):
         """Time the built sort configurations on a copy of the pairs; the
         fastest is used by later sorts of this size class.  Returns
@@ -339,6 +412,23 @@ class Context:
         self._chk(lib().gb_radix_autotune(self.h, keys_ptr, vals_ptr, n, bits, ctypes.byref(p), ctypes.byref(it),
                                           ctypes.byref(ms)))
         return p.value, it.value, ms.value
+
+
+def _device_boxes(boxes):
+    import torch
+    if isinstance(boxes, torch.Tensor):
+        return boxes.to(device="cuda", dtype=torch.int32).contiguous().view(-1, 4)
+    return torch.from_numpy(_boxes(boxes).copy()).cuda()
+
+
+def snap_file_info(path):
+    """(total boxes, chunks, compression method, layer properties) of a .snap file."""
+    n, c = ctypes.c_int64(), ctypes.c_int64()
+    m, p = ctypes.c_int(), ctypes.c_int()
+    rc = lib().gb_snap_file_info(os.fsencode(path), ctypes.byref(n), ctypes.byref(c), ctypes.byref(m), ctypes.byref(p))
+    if rc != GB_OK:
+        raise GBError(rc, "gb_snap_file_info failed for %s" % path)
+    return n.value, c.value, m.value, p.value
 
 
 # ---- the reference's own FFI, called exactly as the Fortran layer calls it
