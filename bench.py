@@ -318,6 +318,94 @@ def run_reference(args, boxes, off, world, rank, dist):
     }), flush=True)
 
 
+def snap_leg(n_per=10_000_000, steps=3, cpu_chunks=96):
+    """SNAP layer streams (box codec + Snappy per 65536-box chunk, the
+    SaveLayerToSnap / RestoreSnapToLayer path) on a Morton-sorted standard-
+    cell layer (4 layers x n_per boxes + 2% contacts in a 4e7 die):
+    device-resident gb_compress_boxes_to_stream and
+    gb_decompress_stream_to_boxes (method 1, Snappy), timed with CUDA events,
+    the round trip checked; then the oracle on all host cores over a sample
+    of chunks (chunks in parallel, as the reference's OpenMP loop).
+    Algorithmic bytes: encode 16 B/box read + codec bytes written and read +
+    Snappy bytes written; decode the same in reverse."""
+    import concurrent.futures as cf
+    import ctypes
+    import torch
+    from vlsi_layout_gb300 import engine
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import gen
+    L = engine.lib()
+    sc = gen.stdcell_layers(n_per, die=40_000_000, seed=1)
+    B = np.concatenate([sc[k] for k in ("poly", "met1", "met2", "li1", "contact")])
+    n = len(B)
+    peak, kind = peaks()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    res = {"n": n, "method": "snappy", "workload": "stdcell layers (poly, met1, met2, li1 x %d + 2%% contacts, "
+           "4e7 die), Morton sorted" % n_per}
+    with engine.Context(0) as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        d = torch.from_numpy(B).cuda()
+        keys = torch.empty(n, dtype=torch.int64, device="cuda")
+        vals = torch.empty(n, dtype=torch.int32, device="cuda")
+        L.gb_morton_keys_device(ctx.h, d.data_ptr(), n, keys.data_ptr(), vals.data_ptr())
+        torch.cuda.synchronize()
+        d = d[torch.argsort(keys, stable=True)].contiguous()
+        del keys, vals
+        cap = ctypes.c_int64()
+        L.gb_snap_max_bytes(n, ctypes.byref(cap))
+        out = torch.empty(cap.value, dtype=torch.uint8, device="cuda")
+        back = torch.empty_like(d)
+        nch = (n + 65535) // 65536
+        meta = np.zeros(3 * nch, np.int64)
+        tot = ctypes.c_int64()
+        te, td = [], []
+        for it in range(steps + 1):
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            ctx._chk(L.gb_compress_boxes_to_stream(ctx.h, d.data_ptr(), n, 1, out.data_ptr(), cap.value,
+                                                   meta.ctypes.data, ctypes.byref(tot)))
+            e1.record(stream)
+            ctx._chk(L.gb_decompress_stream_to_boxes(ctx.h, out.data_ptr(), meta.ctypes.data, nch, 1,
+                                                     back.data_ptr()))
+            e2.record(stream)
+            torch.cuda.synchronize()
+            if it:
+                te.append(e0.elapsed_time(e1))
+                td.append(e1.elapsed_time(e2))
+        ok = bool(torch.equal(back, d))
+        raw = int(meta[1::3].sum())
+        comp = int(meta[2::3].sum())
+        ms_e, ms_d = statistics.median(te), statistics.median(td)
+        byts = 16 * n + 2 * raw + comp
+        res.update({"raw_bytes_per_box": raw / n, "compressed_bytes_per_box": comp / n, "round_trip_ok": ok,
+                    "encode_ms": ms_e, "decode_ms": ms_d,
+                    "encode_boxes_per_s": n / (ms_e / 1e3), "decode_boxes_per_s": n / (ms_d / 1e3),
+                    "encode_frac_of_peak": byts / (ms_e / 1e3) / 1e9 / peak,
+                    "decode_frac_of_peak": byts / (ms_d / 1e3) / 1e9 / peak})
+        B = d[:cpu_chunks * 65536].cpu().numpy()
+    del d, out, back
+    torch.cuda.empty_cache()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    parts = [B[i:i + 65536] for i in range(0, len(B), 65536)]
+    cores = os.cpu_count() or 1
+
+    with cf.ThreadPoolExecutor(cores) as ex:
+        t0 = time.perf_counter()
+        encs = list(ex.map(lambda p: O.stream_encode(p, 1), parts))
+        t1 = time.perf_counter()
+        decs = list(ex.map(lambda c: O.stream_decode(c, 1), encs))
+        t2 = time.perf_counter()
+    assert all(np.array_equal(a, b) for a, b in zip(decs, parts))
+    res["cpu_baseline"] = {"encode_boxes_per_s": len(B) / (t1 - t0), "decode_boxes_per_s": len(B) / (t2 - t1),
+                           "cores": cores, "kind": "port",
+                           "sample": "first %d chunks (%d boxes), one chunk per thread" % (len(parts), len(B))}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,12 +427,20 @@ def main():
     ap.add_argument("--sort-n", type=int, default=200_000_000)
     ap.add_argument("--no-sort", action="store_true")
     ap.add_argument("--sort-no-tune", action="store_true", help="time the default sort plan only")
+    ap.add_argument("--snap-only", action="store_true")
+    ap.add_argument("--no-snap", action="store_true")
+    ap.add_argument("--snap-n", type=int, default=10_000_000, help="boxes per stdcell layer of the SNAP leg")
     args = ap.parse_args()
     world, rank, local, dist = dist_init()
     if args.sort_only:
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps, tune=not args.sort_no_tune)}), flush=True)
+        return
+    if args.snap_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"snap": snap_leg(n_per=args.snap_n, steps=args.steps)}), flush=True)
         return
     if args.serve_only:
         import torch
@@ -481,6 +577,9 @@ def main():
     sort = None
     if rank == 0 and not args.no_sort:
         sort = sort_leg(n=args.sort_n, steps=3)
+    snap = None
+    if rank == 0 and not args.no_snap:
+        snap = snap_leg(n_per=args.snap_n, steps=3)
     value = replica_value(world, nbox, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
@@ -509,6 +608,7 @@ def main():
         "parity": parity,
         "serving": serving,
         "sort": sort,
+        "snap": snap,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -261,8 +261,10 @@ int64_t orc_snappy_max_length(int64_t len) { return 32 + len + len / 6; }
 // ((v * 0x9E3779B1) >> 20, Knuth's multiplicative hash into 4096 slots;
 // every position is hashed, including those inside matches).  The parse
 // starts at 0; at p, when the candidate's 4 bytes equal those at p, the match
-// is extended as far as the fragment allows and emitted (pending literal
-// first) and p jumps past it; otherwise p advances by one.  Copies are split
+// is extended as far as the fragment allows and, when at least 8 bytes long,
+// emitted (pending literal first) and p jumps past it; otherwise p advances
+// by one.  (Shorter matches save at most a few bytes but add elements, which
+// a decoder has to take one after another.)  Copies are split
 // into pieces of 64 (60 when 65..67 remain), each piece a 1-byte-offset copy
 // when 4..11 long with offset < 2048, else a 2-byte-offset copy.
 int64_t orc_snappy_compress(const uint8_t* in, int64_t len, uint8_t* out) {
@@ -284,13 +286,15 @@ int64_t orc_snappy_compress(const uint8_t* in, int64_t len, uint8_t* out) {
         const int64_t q = c - 1;
         int64_t L = 4;
         while (p + L < fl && s[q + L] == s[p + L]) ++L;
-        if (p > lit) o += emit_literal(out + o, s + lit, p - lit);
-        o += emit_copy(out + o, (uint32_t)(p - q), L);
-        p += L;
-        lit = p;
-      } else {
-        ++p;
+        if (L >= 8) {
+          if (p > lit) o += emit_literal(out + o, s + lit, p - lit);
+          o += emit_copy(out + o, (uint32_t)(p - q), L);
+          p += L;
+          lit = p;
+          continue;
+        }
       }
+      ++p;
     }
     if (fl > lit) o += emit_literal(out + o, s + lit, fl - lit);
   }

@@ -67,12 +67,14 @@ def cases(big=False):
     c["stdcell"] = np.concatenate([sc[k] for k in ("poly", "met1", "met2", "li1", "contact")])
     c["chunk_exact"] = gen.random_layer(65536, seed=4)
     c["chunk_plus_one"] = gen.random_layer(65537, seed=5)
-    # 5000 distinct widths in one chunk: more than a shared-memory table holds
-    w = rng.integers(1, 5001, 20000)
-    h = rng.integers(1, 300, 20000)
-    x = rng.integers(-1000000, 1000000, 20000)
-    y = rng.integers(-1000000, 1000000, 20000)
-    c["many_widths"] = np.stack([x, y, x + w, y + h], 1).astype(np.int32)
+    # about 5000 distinct widths in one chunk (a shared-memory table), and
+    # about 17000 (more than it holds: the global-memory table)
+    for name, wmax, nbx in (("many_widths", 5001, 20000), ("more_widths", 30001, 30000)):
+        w = rng.integers(1, wmax, nbx)
+        h = rng.integers(1, 300, nbx)
+        x = rng.integers(-1000000, 1000000, nbx)
+        y = rng.integers(-1000000, 1000000, nbx)
+        c[name] = np.stack([x, y, x + w, y + h], 1).astype(np.int32)
     if big:
         c["macros"] = gen.macro_arrays(nmacro=40, seed=9)
         c["random_300k"] = gen.random_layer(300000, seed=6)

@@ -6,12 +6,12 @@
 // RestoreCompressedStreamFromDisk).
 //
 // Encoding, per chunk (one 1024-thread CTA):
-//   * widths, and heights of the non-square boxes, go into open-addressing
-//     tables (shared memory; a chunk with more than 2048 distinct values is
-//     redone with 131072-slot tables in global memory) that keep each value's
-//     first position; a bitmap of first positions with prefix popcounts gives
-//     each value its 1-based order of first appearance, which is the codec's
-//     dictionary index;
+//   * widths, then heights of the non-square boxes, go into an open-addressing
+//     table (16384 slots in shared memory; a chunk with more than 8192
+//     distinct values is redone with a 131072-slot table in global memory)
+//     that keeps each value's first position; a bitmap of first positions
+//     with prefix popcounts gives each value its 1-based order of first
+//     appearance, the codec's dictionary index, stored per box;
 //   * boxes are then taken in order, 1024 at a time: a box's record (infobyte,
 //     zigzag varint anchor deltas, the width / height as a varint when new or
 //     an int16 index when seen before) depends only on the previous box, the
@@ -22,13 +22,15 @@
 // one warp, 32 positions at a time: a position's candidate is the latest
 // earlier position with the same 12-bit hash of its 4 bytes (warp match for
 // the batch, a 4096-slot table across batches); the greedy parse jumps to
-// the next verified candidate, extends the match 32 bytes per step and emits
-// Snappy literal / copy elements.  Fragments are concatenated behind the
+// the next verified candidate, extends the match 32 bytes per step and, when
+// it is at least 8 bytes long, emits Snappy literal / copy elements.  Fragments are concatenated behind the
 // chunk's length preamble.  Decoding takes one warp per chunk through the
-// elements (all element forms of the format are accepted).
-// Decoding the codec: one warp per chunk finds the record boundaries (all
-// lanes compute the length a record would have at each byte of a 1 KB
-// window, one lane walks the chain), then one CTA per chunk parses the
+// elements (all element forms of the format are accepted), with the last
+// 64 KB of output in a shared-memory ring for the copies.
+// Decoding the codec: one CTA per chunk finds the record boundaries (all
+// threads compute the length a record would have at each byte of a 4 KB
+// window, and the lengths of the next four records from there; one thread
+// walks the chain four records per load), then one CTA per chunk parses the
 // records 1024 at a time, rebuilds the anchors and dictionary indices with
 // block scans and gathers widths and heights from per-chunk dictionaries.
 #include <cstdio>
@@ -42,11 +44,9 @@
 #define SN_FRAG 65536   // Snappy fragment (bytes)
 #define SN_FCAP (SN_FRAG + SN_FRAG / 6 + 64)
 #define SN_T 1024       // threads of the per-chunk CTAs
-#define SN_STAB_LOG 12  // shared tables: 4096 slots, at most 2048 distinct values
-#define SN_GTAB_LOG 17  // global tables: 131072 slots
 #define SN_REC_MAX 31   // longest record of a valid box (1 + 5 + 5 + 10 + 10)
-#define SN_WIN 1024     // boundary window (bytes)
 #define SN_WPAD 64      // look-ahead behind the window
+#define SN_MIN_MATCH 8  // shortest copy the compressor emits
 #define SN_CODEC_VERSION 1
 #define SN_LAYER_STATE_PNUM 4
 #define KID_SNAP_ENC 60
@@ -154,49 +154,51 @@ __device__ __forceinline__ T block_excl(T x, T ident, T* buf, T* tot) {
   return wid ? op(buf[wid - 1], ex) : ex;
 }
 
-// ---------------------------------------------------------------- encoder tables
-struct SnTab {
-  unsigned long long* key;  // (1 << 32) | value; 0 = empty
-  unsigned* pos;            // first position in the chunk
-  int log;
-  unsigned* ndist;          // distinct values inserted
-  unsigned limit;           // refuse new values beyond this many
-};
+// ---------------------------------------------------------------- encoder: dictionary ranks
+// Open-addressing table of one chunk: slot = (first position << 32) | value,
+// empty = all ones (positions are below 65536, so an occupied slot never has
+// an all-ones high word).  Inserting an existing value lowers its position
+// with atomicMin on the whole word, which keeps the value.
+#define SN_EMPTY 0xffffffffffffffffull
+#define SN_STAB_SLOTS 16384  // shared table: at most 8192 distinct values
+#define SN_GTAB_SLOTS 131072 // global table (a chunk has at most 65536 values)
 
-__device__ __forceinline__ unsigned sn_slot(int v, int log) { return ((unsigned)v * 0x9E3779B1u) >> (32 - log); }
+__device__ __forceinline__ unsigned sn_slot(int v, unsigned mask) { return ((unsigned)v * 0x9E3779B1u >> 15) & mask; }
 
-// slot of v (inserted when absent); -1 when the table is at its limit
-__device__ int tab_insert(const SnTab& t, int v) {
-  const unsigned long long k = (1ull << 32) | (unsigned)v;
-  const unsigned mask = (1u << t.log) - 1u;
-  unsigned s = sn_slot(v, t.log);
+// inserts (v, j); false when the table holds `limit` values already
+__device__ __forceinline__ bool tab_insert(unsigned long long* tab, unsigned mask, int v, unsigned j,
+                                           unsigned* ndist, unsigned limit) {
+  const unsigned long long mine = ((unsigned long long)j << 32) | (unsigned)v;
+  unsigned s = sn_slot(v, mask);
   for (unsigned probe = 0; probe <= mask; ++probe) {
-    unsigned long long cur = *(volatile unsigned long long*)&t.key[s];
-    if (cur == 0) {
-      if (*(volatile unsigned*)t.ndist >= t.limit) return -1;
-      cur = atomicCAS(&t.key[s], 0ull, k);
-      if (cur == 0) {
-        atomicAdd(t.ndist, 1u);
-        return (int)s;
+    unsigned long long cur = *(volatile unsigned long long*)&tab[s];
+    if (cur == SN_EMPTY) {
+      if (*(volatile unsigned*)ndist >= limit) return false;
+      cur = atomicCAS(&tab[s], SN_EMPTY, mine);
+      if (cur == SN_EMPTY) {
+        atomicAdd(ndist, 1u);
+        return true;
       }
     }
-    if (cur == k) return (int)s;
+    if ((unsigned)cur == (unsigned)v) {
+      if ((unsigned)(cur >> 32) > j) atomicMin(&tab[s], mine);
+      return true;
+    }
     s = (s + 1u) & mask;
   }
-  return -1;
+  return false;
 }
 
-__device__ int tab_find(const SnTab& t, int v) {
-  const unsigned long long k = (1ull << 32) | (unsigned)v;
-  const unsigned mask = (1u << t.log) - 1u;
-  unsigned s = sn_slot(v, t.log);
+// first position of v (the value must be in the table)
+__device__ __forceinline__ unsigned tab_first(const unsigned long long* tab, unsigned mask, int v) {
+  unsigned s = sn_slot(v, mask);
   for (unsigned probe = 0; probe <= mask; ++probe) {
-    const unsigned long long cur = *(volatile unsigned long long*)&t.key[s];
-    if (cur == k) return (int)s;
-    if (cur == 0) return -1;
+    const unsigned long long cur = *(const volatile unsigned long long*)&tab[s];
+    if (cur == SN_EMPTY) break;
+    if ((unsigned)cur == (unsigned)v) return (unsigned)(cur >> 32);
     s = (s + 1u) & mask;
   }
-  return -1;
+  return 0xffffffffu;
 }
 
 // 1-based order of first appearance of the value first seen at position p
@@ -204,221 +206,197 @@ __device__ __forceinline__ unsigned sn_rank(const unsigned* bits, const unsigned
   return pre[p >> 5] + __popc(bits[p >> 5] & ((1u << (p & 31)) - 1u)) + 1u;
 }
 
-// Codec encoder, one CTA per chunk.  GT: tables in global memory (chunks
-// listed in `list`), else in shared memory (chunk = block index; chunks
-// whose tables overflow are appended to ovf_list).  WRITE: emit the bytes at
-// raw + raw_off[c], else store the chunk's byte count in raw_size[c].
-template <bool GT, bool WRITE>
+// Dictionary ranks of one chunk per CTA: ranks[b] (widths) and ranks[n + b]
+// (heights of non-square boxes) = order of first appearance | first << 31.
+// The width table is built and read, then the height table in the same
+// storage.  GT: 131072-slot tables in global memory for the chunks in list
+// (one table per CTA), else 16384-slot shared tables (chunk = block index);
+// a chunk with more values than a shared table holds goes to ovf_list.
+template <bool GT>
 __global__ void __launch_bounds__(SN_T, 1)
-k_codec_encode(const int4* __restrict__ boxes, long long n, const int* __restrict__ list, int nlist,
-               unsigned long long* gkeys, unsigned* gpos, long long* raw_size, const long long* __restrict__ raw_off,
-               unsigned char* __restrict__ raw, int* ovf_list, int* ovf_count, DStatus* st) {
+k_enc_rank(const int4* __restrict__ boxes, long long n, const int* __restrict__ list, int nlist,
+           unsigned long long* gtab, unsigned* __restrict__ ranks, int* ovf_list, int* ovf_count, DStatus* st) {
   extern __shared__ __align__(16) unsigned char sm[];
-  constexpr int LOG = GT ? SN_GTAB_LOG : SN_STAB_LOG;
-  constexpr int CAP = 1 << LOG;
+  constexpr unsigned SLOTS = GT ? SN_GTAB_SLOTS : SN_STAB_SLOTS;
+  constexpr unsigned MASK = SLOTS - 1u;
+  constexpr unsigned LIMIT = GT ? SLOTS : SLOTS / 2;
   unsigned char* q = sm;
-  unsigned long long *wkey, *hkey;
-  unsigned *wpos, *hpos;
+  unsigned long long* tab;
   if (GT) {
-    wkey = gkeys + (size_t)blockIdx.x * 2 * CAP;
-    hkey = wkey + CAP;
-    wpos = gpos + (size_t)blockIdx.x * 2 * CAP;
-    hpos = wpos + CAP;
+    tab = gtab + (size_t)blockIdx.x * SLOTS;
   } else {
-    wkey = (unsigned long long*)q;
-    hkey = wkey + CAP;
-    q += 2 * CAP * 8;
-    wpos = (unsigned*)q;
-    hpos = wpos + CAP;
-    q += 2 * CAP * 4;
+    tab = (unsigned long long*)q;
+    q += SLOTS * 8;
   }
-  unsigned* wbit = (unsigned*)q;  // [2048] first-position bitmaps
-  unsigned* hbit = wbit + 2048;
-  unsigned* wpre = hbit + 2048;   // [2048] exclusive popcounts
-  unsigned* hpre = wpre + 2048;
-  SumS* bufS = (SumS*)(hpre + 2048);        // [2][32]
-  LastS* bufL = (LastS*)(bufS + 64);        // [2][32]
-  Last2* bufP = (Last2*)(bufL + 64);        // [32] (bitmap prefix pairs)
-  unsigned* flags = (unsigned*)(bufP + 32); // nw, nh, overflow
-  const int t = threadIdx.x;
+  unsigned* bits = (unsigned*)q;  // [2048] first-position bitmap
+  unsigned* pre = bits + 2048;    // [2048] exclusive popcounts
+  int* wsum = (int*)(pre + 2048); // [32]
+  unsigned* flags = (unsigned*)(wsum + 32);  // distinct values, overflow
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const long long nchunks = (n + SN_CHUNK - 1) / SN_CHUNK;
   const long long nitems = GT ? nlist : nchunks;
   for (long long li = blockIdx.x; li < nitems; li += gridDim.x) {
     const long long c = GT ? list[li] : li;
     const long long b0 = c * SN_CHUNK;
     const int nb = (int)min((long long)SN_CHUNK, n - b0);
-    for (int i = t; i < CAP; i += SN_T) {
-      wkey[i] = 0;
-      hkey[i] = 0;
-      wpos[i] = 0xffffffffu;
-      hpos[i] = 0xffffffffu;
-    }
-    for (int i = t; i < 2048; i += SN_T) {
-      wbit[i] = 0;
-      hbit[i] = 0;
-    }
-    if (t < 3) flags[t] = 0;
-    if (GT) __threadfence_block();
-    __syncthreads();
-    const unsigned lim = GT ? (unsigned)CAP : (unsigned)(CAP / 2);
-    const SnTab W{wkey, wpos, LOG, &flags[0], lim};
-    const SnTab H{hkey, hpos, LOG, &flags[1], lim};
-    for (int j = t; j < nb; j += SN_T) {
-      const int4 b = boxes[b0 + j];
-      const int w = (int)((unsigned)b.z - (unsigned)b.x), h = (int)((unsigned)b.w - (unsigned)b.y);
-      int s = tab_insert(W, w);
-      if (s < 0) {
-        flags[2] = 1;
-        break;
-      }
-      atomicMin(&wpos[s], (unsigned)j);
-      if (w != h) {
-        s = tab_insert(H, h);
-        if (s < 0) {
-          flags[2] = 1;
+    bool ovf = false;
+    for (int which = 0; which < 2 && !ovf; ++which) {
+      for (unsigned i = t; i < SLOTS; i += SN_T) tab[i] = SN_EMPTY;
+      for (int i = t; i < 2048; i += SN_T) bits[i] = 0;
+      if (t < 2) flags[t] = 0;
+      __syncthreads();
+      for (int j = t; j < nb; j += SN_T) {
+        const int4 b = boxes[b0 + j];
+        const int w = (int)((unsigned)b.z - (unsigned)b.x), h = (int)((unsigned)b.w - (unsigned)b.y);
+        if (which && w == h) continue;
+        if (!tab_insert(tab, MASK, which ? h : w, (unsigned)j, &flags[0], LIMIT)) {
+          flags[1] = 1;
           break;
         }
-        atomicMin(&hpos[s], (unsigned)j);
-      }
-    }
-    __syncthreads();
-    const bool ovf = *(volatile unsigned*)&flags[2] != 0;
-    if (ovf) {
-      if (t == 0) {
-        if (GT)
-          gb_set_error(st, GB_ERR_INTERNAL, KID_SNAP_ENC, c);
-        else
-          ovf_list[atomicAdd(ovf_count, 1)] = (int)c;
       }
       __syncthreads();
-      continue;
-    }
-    for (int i = t; i < CAP; i += SN_T) {
-      if (*(volatile unsigned long long*)&wkey[i]) {
-        const unsigned pp = *(volatile unsigned*)&wpos[i];
-        atomicOr(&wbit[pp >> 5], 1u << (pp & 31));
-      }
-      if (*(volatile unsigned long long*)&hkey[i]) {
-        const unsigned pp = *(volatile unsigned*)&hpos[i];
-        atomicOr(&hbit[pp >> 5], 1u << (pp & 31));
-      }
-    }
-    __syncthreads();
-    {  // exclusive popcount prefixes of the two bitmaps (two words per thread)
-      const int pw = __popc(wbit[2 * t]) + __popc(wbit[2 * t + 1]);
-      const int ph = __popc(hbit[2 * t]) + __popc(hbit[2 * t + 1]);
-      // bufP holds the warps' (width, height) popcount sums
-      const int lane = t & 31, wid = t >> 5;
-      int iw = pw, ih = ph;
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int ow = __shfl_up_sync(0xffffffffu, iw, d), oh = __shfl_up_sync(0xffffffffu, ih, d);
-        if (lane >= d) {
-          iw += ow;
-          ih += oh;
+      ovf = *(volatile unsigned*)&flags[1] != 0;
+      if (ovf) break;  // uniform
+      for (unsigned i = t; i < SLOTS; i += SN_T) {
+        const unsigned long long cur = *(volatile unsigned long long*)&tab[i];
+        if (cur != SN_EMPTY) {
+          const unsigned p = (unsigned)(cur >> 32);
+          atomicOr(&bits[p >> 5], 1u << (p & 31));
         }
       }
-      if (lane == 31) bufP[wid] = {iw, ih};
       __syncthreads();
-      if (wid == 0) {
-        int vw = bufP[lane].w, vh = bufP[lane].h;
+      {  // exclusive popcount prefix, two words per thread
+        const int pc = __popc(bits[2 * t]) + __popc(bits[2 * t + 1]);
+        int inc = pc;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-          const int ow = __shfl_up_sync(0xffffffffu, vw, d), oh = __shfl_up_sync(0xffffffffu, vh, d);
-          if (lane >= d) {
-            vw += ow;
-            vh += oh;
-          }
+          const int o = __shfl_up_sync(0xffffffffu, inc, d);
+          if (lane >= d) inc += o;
         }
-        bufP[lane] = {vw, vh};
+        if (lane == 31) wsum[wid] = inc;
+        __syncthreads();
+        if (wid == 0) {
+          int v = wsum[lane];
+#pragma unroll
+          for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(0xffffffffu, v, d);
+            if (lane >= d) v += o;
+          }
+          wsum[lane] = v;
+        }
+        __syncthreads();
+        const int ex = inc - pc + (wid ? wsum[wid - 1] : 0);
+        pre[2 * t] = (unsigned)ex;
+        pre[2 * t + 1] = (unsigned)ex + __popc(bits[2 * t]);
       }
       __syncthreads();
-      const int ew = iw - pw + (wid ? bufP[wid - 1].w : 0), eh = ih - ph + (wid ? bufP[wid - 1].h : 0);
-      wpre[2 * t] = (unsigned)ew;
-      wpre[2 * t + 1] = (unsigned)ew + __popc(wbit[2 * t]);
-      hpre[2 * t] = (unsigned)eh;
-      hpre[2 * t + 1] = (unsigned)eh + __popc(hbit[2 * t]);
+      unsigned* out = ranks + (which ? n : 0) + b0;
+      for (int j = t; j < nb; j += SN_T) {
+        const int4 b = boxes[b0 + j];
+        const int w = (int)((unsigned)b.z - (unsigned)b.x), h = (int)((unsigned)b.w - (unsigned)b.y);
+        if (which && w == h) continue;
+        const unsigned p = tab_first(tab, MASK, which ? h : w);
+        if (p >= SN_CHUNK) {
+          gb_set_error(st, GB_ERR_INTERNAL, KID_SNAP_ENC, b0 + j);
+          continue;
+        }
+        out[j] = sn_rank(bits, pre, p) | ((p == (unsigned)j) ? 0x80000000u : 0u);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    unsigned long long cbytes = 0;  // bytes of the records so far
-    LastS chl{0, 0};                // last non-square box's height so far
-    unsigned char* out = WRITE ? raw + raw_off[c] : nullptr;
-    for (int k = 0; k * SN_T < nb; ++k) {
-      const int j = k * SN_T + t;
-      const bool valid = j < nb;
-      int4 b = make_int4(0, 0, 0, 0), pb = make_int4(0, 0, 0, 0);
-      if (valid) {
-        b = boxes[b0 + j];
-        if (j) pb = boxes[b0 + j - 1];
-      }
-      const int w = (int)((unsigned)b.z - (unsigned)b.x), h = (int)((unsigned)b.w - (unsigned)b.y);
-      const bool sq = w == h;
-      LastS tl;
-      LastS ph = block_excl(LastS{valid && !sq, h}, LastS{0, 0}, bufL + 32 * (k & 1), &tl);
-      ph = op(chl, ph);
-      unsigned info = 0, size = 0, wr = 0, hr = 0;
-      bool wnew = false, hnew = false;
-      int dx = 0, dy = 0;
-      if (valid) {
-        const int pw = j ? (int)((unsigned)pb.z - (unsigned)pb.x) : 0;
-        dx = (int)((unsigned)b.x - (unsigned)pb.x);  // the anchor cursor starts at 0 and follows x1
-        dy = (int)((unsigned)b.y - (unsigned)pb.y);
-        if (sq) info |= 16;
-        if (dx) info |= 32;
-        if (dy) info |= 64;
-        const int ws = tab_find(W, w);
-        const unsigned wp = ws >= 0 ? *(volatile unsigned*)&wpos[ws] : 0u;
-        wnew = wp == (unsigned)j;
-        wr = sn_rank(wbit, wpre, wp);
-        if (j == 0 || w != pw) info |= wnew ? 3u : 1u;
-        if (!sq) {
-          const int hs = tab_find(H, h);
-          const unsigned hp = hs >= 0 ? *(volatile unsigned*)&hpos[hs] : 0u;
-          hnew = hp == (unsigned)j;
-          hr = sn_rank(hbit, hpre, hp);
-          if (!ph.has || ph.val != h) info |= hnew ? 12u : 4u;
-        }
-        if (ws < 0) gb_set_error(st, GB_ERR_INTERNAL, KID_SNAP_ENC, b0 + j);
-        size = 1;
-        if (info & 32) size += sn_vlen(sn_zigzag(dx));
-        if (info & 64) size += sn_vlen(sn_zigzag(dy));
-        if (info & 1) size += (info & 2) ? sn_vlen((unsigned long long)(long long)w) : 2;
-        if (info & 4) size += (info & 8) ? sn_vlen((unsigned long long)(long long)h) : 2;
-      }
-      SumS ts;
-      const SumS ex = block_excl(SumS{size}, SumS{0}, bufS + 32 * (k & 1), &ts);
-      if (WRITE && valid) {
-        unsigned char* o = out + cbytes + ex.a;
-        *o++ = (unsigned char)info;
-        if (info & 32) o = sn_put_varint(o, sn_zigzag(dx));
-        if (info & 64) o = sn_put_varint(o, sn_zigzag(dy));
-        if (info & 1) {
-          if (info & 2) {
-            o = sn_put_varint(o, (unsigned long long)(long long)w);
-          } else {
-            *o++ = (unsigned char)wr;
-            *o++ = (unsigned char)(wr >> 8);
-          }
-        }
-        if (info & 4) {
-          if (info & 8) {
-            o = sn_put_varint(o, (unsigned long long)(long long)h);
-          } else {
-            *o++ = (unsigned char)hr;
-            *o++ = (unsigned char)(hr >> 8);
-          }
-        }
-      }
-      cbytes += ts.a;
-      chl = op(chl, tl);
-    }
-    if (t == 0) {
-      if (!WRITE)
-        raw_size[c] = (long long)cbytes;
-      else if ((long long)cbytes != raw_off[c + 1] - raw_off[c])
+    if (ovf && t == 0) {
+      if (GT)
         gb_set_error(st, GB_ERR_INTERNAL, KID_SNAP_ENC, c);
+      else
+        ovf_list[atomicAdd(ovf_count, 1)] = (int)c;
     }
     __syncthreads();
+  }
+}
+
+// Codec records of one chunk per CTA from the ranks: WRITE emits the bytes
+// at raw + raw_off[c], else raw_size[c] receives the chunk's byte count.
+template <bool WRITE>
+__global__ void __launch_bounds__(SN_T, 1)
+k_enc_emit(const int4* __restrict__ boxes, long long n, const unsigned* __restrict__ ranks,
+           long long* raw_size, const long long* __restrict__ raw_off, unsigned char* __restrict__ raw, DStatus* st) {
+  __shared__ SumS bufS[2][32];
+  __shared__ LastS bufL[2][32];
+  const long long c = blockIdx.x;
+  const int t = threadIdx.x;
+  const long long b0 = c * SN_CHUNK;
+  const int nb = (int)min((long long)SN_CHUNK, n - b0);
+  unsigned long long cbytes = 0;  // bytes of the records so far
+  LastS chl{0, 0};                // last non-square box's height so far
+  unsigned char* out = WRITE ? raw + raw_off[c] : nullptr;
+  for (int k = 0; k * SN_T < nb; ++k) {
+    const int j = k * SN_T + t;
+    const bool valid = j < nb;
+    int4 b = make_int4(0, 0, 0, 0), pb = make_int4(0, 0, 0, 0);
+    if (valid) {
+      b = boxes[b0 + j];
+      if (j) pb = boxes[b0 + j - 1];
+    }
+    const int w = (int)((unsigned)b.z - (unsigned)b.x), h = (int)((unsigned)b.w - (unsigned)b.y);
+    const bool sq = w == h;
+    LastS tl;
+    LastS ph = block_excl(LastS{valid && !sq, h}, LastS{0, 0}, bufL[k & 1], &tl);
+    ph = op(chl, ph);
+    unsigned info = 0, size = 0, wr = 0, hr = 0;
+    int dx = 0, dy = 0;
+    if (valid) {
+      const int pw = j ? (int)((unsigned)pb.z - (unsigned)pb.x) : 0;
+      dx = (int)((unsigned)b.x - (unsigned)pb.x);  // the anchor cursor starts at 0 and follows x1
+      dy = (int)((unsigned)b.y - (unsigned)pb.y);
+      if (sq) info |= 16;
+      if (dx) info |= 32;
+      if (dy) info |= 64;
+      const unsigned rw = ranks[b0 + j];
+      wr = rw & 0x7fffffffu;
+      if (j == 0 || w != pw) info |= (rw >> 31) ? 3u : 1u;
+      if (!sq) {
+        const unsigned rh = ranks[n + b0 + j];
+        hr = rh & 0x7fffffffu;
+        if (!ph.has || ph.val != h) info |= (rh >> 31) ? 12u : 4u;
+      }
+      size = 1;
+      if (info & 32) size += sn_vlen(sn_zigzag(dx));
+      if (info & 64) size += sn_vlen(sn_zigzag(dy));
+      if (info & 1) size += (info & 2) ? sn_vlen((unsigned long long)(long long)w) : 2;
+      if (info & 4) size += (info & 8) ? sn_vlen((unsigned long long)(long long)h) : 2;
+    }
+    SumS ts;
+    const SumS ex = block_excl(SumS{size}, SumS{0}, bufS[k & 1], &ts);
+    if (WRITE && valid) {
+      unsigned char* o = out + cbytes + ex.a;
+      *o++ = (unsigned char)info;
+      if (info & 32) o = sn_put_varint(o, sn_zigzag(dx));
+      if (info & 64) o = sn_put_varint(o, sn_zigzag(dy));
+      if (info & 1) {
+        if (info & 2) {
+          o = sn_put_varint(o, (unsigned long long)(long long)w);
+        } else {  // int16 index, little-endian (wraps above 32767 as the reference's int16 does)
+          *o++ = (unsigned char)wr;
+          *o++ = (unsigned char)(wr >> 8);
+        }
+      }
+      if (info & 4) {
+        if (info & 8) {
+          o = sn_put_varint(o, (unsigned long long)(long long)h);
+        } else {
+          *o++ = (unsigned char)hr;
+          *o++ = (unsigned char)(hr >> 8);
+        }
+      }
+    }
+    cbytes += ts.a;
+    chl = op(chl, tl);
+  }
+  if (t == 0) {
+    if (!WRITE)
+      raw_size[c] = (long long)cbytes;
+    else if ((long long)cbytes != raw_off[c + 1] - raw_off[c])
+      gb_set_error(st, GB_ERR_INTERNAL, KID_SNAP_ENC, c);
   }
 }
 
@@ -458,55 +436,83 @@ __device__ __forceinline__ int sn_rec_len(const unsigned char* p) {
   return l;
 }
 
-// One warp per chunk: rec[c * SN_CHUNK + r] = offset of record r in the chunk.
-__global__ void __launch_bounds__(128)
+// One 256-thread CTA per chunk: rec[c * SN_CHUNK + r] = offset of record r in
+// the chunk.  Per 4 KB window every thread computes the length a record
+// would have at each of its bytes, then, per byte, the lengths of the four
+// records a chain starting there would have (one word); thread 0 walks the
+// chain four records per shared-memory load.
+#define SN_BT 256
+#define SN_BWIN 4096
+#define SN_BPAD 256  // lengths are needed up to three records (3 * 41 bytes) past the window
+__global__ void __launch_bounds__(SN_BT)
 k_codec_bounds(const unsigned char* __restrict__ raw, const long long* __restrict__ raw_off,
                const long long* __restrict__ raw_len, long long n, long long nchunks, unsigned* __restrict__ rec,
                DStatus* st) {
-  __shared__ unsigned char buf[4][SN_WIN + SN_WPAD];
-  __shared__ unsigned char lenb[4][SN_WIN];
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long c = (long long)blockIdx.x * 4 + wid;
-  if (c >= nchunks || *(volatile int*)&st->err) return;
+  __shared__ unsigned char buf[SN_BWIN + SN_BPAD + SN_WPAD];
+  __shared__ unsigned char lenb[SN_BWIN + SN_BPAD];
+  __shared__ unsigned quad[SN_BWIN];
+  __shared__ long long s_pos;
+  __shared__ int s_r, s_bad, s_skip;
+  const int t = threadIdx.x;
+  const long long c = blockIdx.x;
+  if (t == 0) s_skip = *(volatile int*)&st->err;  // the Snappy layer was malformed: one read for the whole CTA
+  __syncthreads();
+  if (s_skip) return;
   const int nb = (int)min((long long)SN_CHUNK, n - c * SN_CHUNK);
   const long long L = raw_len[c];
   const unsigned char* base = raw + raw_off[c];
   unsigned* out = rec + c * SN_CHUNK;
   long long pos = 0;
   int r = 0, bad = 0;
-  for (long long ws = 0; r < nb && !bad; ws += SN_WIN) {
+  for (long long ws = 0; r < nb && !bad; ws += SN_BWIN) {
     if (ws >= L) {
       bad = 1;
       break;
     }
-    for (int b = lane; b < SN_WIN + SN_WPAD; b += 32) buf[wid][b] = ws + b < L ? base[ws + b] : 0;
-    __syncwarp();
-    for (int b = lane; b < SN_WIN; b += 32) {
-      const int l = sn_rec_len(&buf[wid][b]);
-      lenb[wid][b] = (unsigned char)l;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      while (r < nb && pos < ws + SN_WIN) {
-        if (pos >= L) {
-          bad = 1;
-          break;
-        }
-        const int l = lenb[wid][pos - ws];
-        if (!l) {
-          bad = 1;
-          break;
-        }
-        out[r++] = (unsigned)pos;
-        pos += l;
+#pragma unroll 4
+    for (int b = t; b < SN_BWIN + SN_BPAD + SN_WPAD; b += SN_BT) buf[b] = ws + b < L ? base[ws + b] : 0;
+    __syncthreads();
+    for (int b = t; b < SN_BWIN + SN_BPAD; b += SN_BT) lenb[b] = (unsigned char)sn_rec_len(&buf[b]);
+    __syncthreads();
+    for (int b = t; b < SN_BWIN; b += SN_BT) {
+      unsigned q = 0;
+      int at = b;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned l = at < SN_BWIN + SN_BPAD ? lenb[at] : 0u;
+        q |= l << (8 * k);
+        if (!l) break;
+        at += (int)l;
       }
+      quad[b] = q;
     }
-    r = __shfl_sync(0xffffffffu, r, 0);
-    pos = __shfl_sync(0xffffffffu, pos, 0);
-    bad = __shfl_sync(0xffffffffu, bad, 0);
-    __syncwarp();
+    __syncthreads();
+    if (t == 0) {
+      while (r < nb && pos < ws + SN_BWIN && !bad) {
+        const unsigned q = quad[pos - ws];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (r >= nb || pos >= ws + SN_BWIN) break;  // later records are found from the next window
+          const unsigned l = (q >> (8 * k)) & 255u;
+          if (pos >= L || !l) {
+            bad = 1;
+            break;
+          }
+          out[r++] = (unsigned)pos;
+          pos += l;
+        }
+      }
+      s_pos = pos;
+      s_r = r;
+      s_bad = bad;
+    }
+    __syncthreads();
+    pos = s_pos;
+    r = s_r;
+    bad = s_bad;
+    __syncthreads();
   }
-  if (lane == 0 && (bad || pos > L)) gb_set_error(st, GB_ERR_CORRUPT, KID_SNAP_BOUNDS, c);
+  if (t == 0 && (bad || pos > L)) gb_set_error(st, GB_ERR_CORRUPT, KID_SNAP_BOUNDS, c);
 }
 
 // One CTA per chunk: records -> boxes.  dict: per chunk 2 * SN_CHUNK ints.
@@ -515,9 +521,12 @@ k_codec_decode(const unsigned char* __restrict__ raw, const long long* __restric
                const unsigned* __restrict__ rec, long long n, int* dict, int4* __restrict__ out, DStatus* st) {
   __shared__ Sum4 bufA[2][32];
   __shared__ Last2 bufB[2][32];
-  if (*(volatile int*)&st->err) return;  // the boundaries (or the Snappy layer) were malformed
+  __shared__ int s_skip;
   const long long c = blockIdx.x;
   const int t = threadIdx.x;
+  if (t == 0) s_skip = *(volatile int*)&st->err;  // the boundaries (or the Snappy layer) were malformed
+  __syncthreads();
+  if (s_skip) return;
   const long long b0 = c * SN_CHUNK;
   const int nb = (int)min((long long)SN_CHUNK, n - b0);
   const unsigned char* base = raw + raw_off[c];
@@ -634,17 +643,17 @@ __device__ __forceinline__ int sn_copy_piece(unsigned char* o, unsigned off, int
   return 3;
 }
 
-// One warp per fragment (4 per CTA).  fsrc / flen: the fragment's bytes in
+// One warp per fragment (8 per CTA).  fsrc / flen: the fragment's bytes in
 // raw; the compressed elements go to fout + f * SN_FCAP, their count to flout.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __restrict__ fsrc,
                   const int* __restrict__ flen, long long nfrag, unsigned char* __restrict__ fout,
                   int* __restrict__ flout, DStatus* st) {
-  extern __shared__ unsigned table[];  // [4][4096]
+  extern __shared__ unsigned short table[];  // [8][4096]: latest position + 1 (positions with 4 bytes left are < 65533)
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long f = (long long)blockIdx.x * 4 + wid;
+  const long long f = (long long)blockIdx.x * 8 + wid;
   if (f >= nfrag) return;
-  unsigned* tab = table + wid * 4096;
+  unsigned short* tab = table + wid * 4096;
   for (int i = lane; i < 4096; i += 32) tab[i] = 0;
   __syncwarp();
   const unsigned char* src = raw + fsrc[f];
@@ -661,7 +670,7 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
     unsigned cand = 0;  // 1-based
     if (has) cand = lower ? (unsigned)(bb + 31 - __clz(lower)) + 1u : tab[h];
     __syncwarp();
-    if (has && (peers >> lane) == 1u) tab[h] = (unsigned)q + 1u;
+    if (has && (peers >> lane) == 1u) tab[h] = (unsigned short)(q + 1);
     __syncwarp();
     const bool ok = has && cand && sn_ld32(src + cand - 1) == v;
     const unsigned okm = __ballot_sync(0xffffffffu, ok);
@@ -685,6 +694,10 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
         }
         L += 32;
       }
+      if (L < SN_MIN_MATCH) {  // too short to pay for an element: literal byte
+        p += 1;
+        continue;
+      }
       // pending literal
       if (p > lit) {
         const int len = p - lit;
@@ -699,6 +712,7 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
           out[o] = (unsigned char)(nb ? (59 + nb) << 2 : mm << 2);
           for (int i = 0; i < nb; ++i) out[o + 1 + i] = (unsigned char)(mm >> (8 * i));
         }
+#pragma unroll 4
         for (int i = lane; i < len; i += 32) out[o + 1 + nb + i] = src[lit + i];
         o += 1 + nb + len;
       }
@@ -732,6 +746,7 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
       out[o] = (unsigned char)(nb ? (59 + nb) << 2 : mm << 2);
       for (int i = 0; i < nb; ++i) out[o + 1 + i] = (unsigned char)(mm >> (8 * i));
     }
+#pragma unroll 4
     for (int i = lane; i < len; i += 32) out[o + 1 + nb + i] = src[lit + i];
     o += 1 + nb + len;
   }
@@ -755,26 +770,44 @@ __global__ void k_snappy_gather(const unsigned char* __restrict__ fout, const in
     for (long long c = threadIdx.x; c < nchunks; c += blockDim.x) sn_put_varint(dst + pre_at[c], (unsigned long long)pre_val[c]);
 }
 
-// One warp per chunk: Snappy raw stream -> codec bytes.
-__global__ void __launch_bounds__(128)
+// One single-warp CTA per chunk: Snappy raw stream -> codec bytes.  The
+// element tags are read from a 4 KB staging copy of the input, literals are
+// copied with four loads in flight per lane, and copies whose source lies in
+// the last 64 KB of output are read from a shared-memory ring of it.
+#define SN_RING 65536
+#define SN_STAGE 4096
+__global__ void __launch_bounds__(32)
 k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* __restrict__ in_off,
                     const long long* __restrict__ in_len, unsigned char* out_all, const long long* __restrict__ out_off,
                     const long long* __restrict__ out_len, long long nchunks, DStatus* st) {
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long c = (long long)blockIdx.x * 4 + wid;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  unsigned char* ring = dsm;           // output byte x at ring[x % SN_RING]
+  unsigned char* stg = dsm + SN_RING;  // input bytes [sb, sb + SN_STAGE)
+  const int lane = threadIdx.x;
+  const long long c = blockIdx.x;
   if (c >= nchunks) return;
   const unsigned char* in = in_all + in_off[c];
   const long long len = in_len[c];
   unsigned char* out = out_all + out_off[c];
   const long long want = out_len[c];
+  long long sb = -(long long)SN_STAGE - 8;
+  auto stage = [&](long long p) {  // bytes p .. p + 7 staged
+    if (p < sb || p + 8 > sb + SN_STAGE) {
+      sb = p;
+      __syncwarp();
+#pragma unroll 4
+      for (int i = lane; i < SN_STAGE; i += 32) stg[i] = sb + i < len ? in[sb + i] : 0;
+      __syncwarp();
+    }
+  };
   int bad = 0;
   long long p = 0, o = 0;
+  stage(0);
   {
     unsigned long long v = 0;
     int k = 0;
-    for (int i = 0; i < 5; ++i) {
-      if (i >= len) break;
-      const unsigned b = in[i];
+    for (int i = 0; i < 5 && i < len; ++i) {
+      const unsigned b = stg[i];
       v |= (unsigned long long)(b & 127u) << (7 * i);
       if (!(b & 128u)) {
         k = i + 1;
@@ -785,7 +818,10 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
     p = k;
   }
   while (!bad && p < len) {
-    const unsigned tag = in[p++];
+    stage(p);
+    const unsigned tag = stg[p - sb];
+    const unsigned char* tb = stg + (p - sb) + 1;  // up to 4 bytes after the tag
+    ++p;
     const unsigned tt = tag & 3u;
     if (tt == 0) {
       long long m = tag >> 2;
@@ -796,7 +832,7 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
           break;
         }
         m = 0;
-        for (int i = 0; i < nb; ++i) m |= (long long)in[p + i] << (8 * i);
+        for (int i = 0; i < nb; ++i) m |= (long long)tb[i] << (8 * i);
         p += nb;
       }
       const long long L = m + 1;
@@ -804,7 +840,22 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
         bad = 1;
         break;
       }
-      for (long long i = lane; i < L; i += 32) out[o + i] = in[p + i];
+      for (long long i0 = 0; i0 < L; i0 += 128) {
+        unsigned char v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const long long i = i0 + u * 32 + lane;
+          v[u] = i < L ? in[p + i] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const long long i = i0 + u * 32 + lane;
+          if (i < L) {
+            out[o + i] = v[u];
+            ring[(o + i) & (SN_RING - 1)] = v[u];
+          }
+        }
+      }
       p += L;
       o += L;
     } else {
@@ -815,7 +866,7 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
           break;
         }
         L = 4 + ((tag >> 2) & 7u);
-        off = ((long long)(tag >> 5) << 8) | in[p];
+        off = ((long long)(tag >> 5) << 8) | tb[0];
         p += 1;
       } else if (tt == 2) {
         if (p + 2 > len) {
@@ -823,7 +874,7 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
           break;
         }
         L = 1 + (tag >> 2);
-        off = (long long)in[p] | ((long long)in[p + 1] << 8);
+        off = (long long)tb[0] | ((long long)tb[1] << 8);
         p += 2;
       } else {
         if (p + 4 > len) {
@@ -831,16 +882,27 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
           break;
         }
         L = 1 + (tag >> 2);
-        off = (long long)in[p] | ((long long)in[p + 1] << 8) | ((long long)in[p + 2] << 16) |
-              ((long long)in[p + 3] << 24);
+        off = (long long)tb[0] | ((long long)tb[1] << 8) | ((long long)tb[2] << 16) | ((long long)tb[3] << 24);
         p += 4;
       }
       if (off == 0 || off > o || o + L > want) {
         bad = 1;
         break;
       }
-      // byte o + i repeats the period [o - off, o): sources were written before this element
-      for (long long i = lane; i < L; i += 32) out[o + i] = out[o - off + (i < off ? i : i % off)];
+      // byte o + i repeats the period [o - off, o): every source precedes this element
+      if (off + L <= SN_RING) {
+        for (long long i = lane; i < L; i += 32) {
+          const unsigned char v = ring[(o - off + (i < off ? i : i % off)) & (SN_RING - 1)];
+          out[o + i] = v;
+          ring[(o + i) & (SN_RING - 1)] = v;
+        }
+      } else {
+        for (long long i = lane; i < L; i += 32) {
+          const unsigned char v = out[o - off + (i < off ? i : i % off)];
+          out[o + i] = v;
+          ring[(o + i) & (SN_RING - 1)] = v;
+        }
+      }
       o += L;
     }
     __syncwarp();
@@ -865,10 +927,7 @@ struct DevMem {  // stream-ordered scratch, freed on scope exit
   }
 };
 
-size_t enc_smem(bool gt) {
-  const size_t tabs = gt ? 0 : (size_t)2 * (1 << SN_STAB_LOG) * 12;
-  return tabs + 4 * 2048 * 4 + 64 * sizeof(SumS) + 64 * sizeof(LastS) + 32 * sizeof(Last2) + 16;
-}
+size_t rank_smem(bool gt) { return (gt ? 0 : (size_t)SN_STAB_SLOTS * 8) + 2 * 2048 * 4 + 32 * 4 + 16; }
 
 long long nchunks_of(long long n) { return (n + SN_CHUNK - 1) / SN_CHUNK; }
 
@@ -883,30 +942,28 @@ int snap_encode(gb_context* ctx, const int4* d_boxes, long long n, int method, u
   DevMem M(c.stream);
   long long* d_rsize = M.get<long long>(nch);
   long long* d_roff = M.get<long long>(nch + 1);
-  int* d_ovf = M.get<int>(2 * (nch + 1));  // [count, list] for the sizing and the writing launch
-  if (!d_rsize || !d_roff || !d_ovf) return gbi::set_err(ctx, GB_ERR_OOM, "snap encode scratch");
-  cudaMemsetAsync(d_ovf, 0, 2 * (nch + 1) * sizeof(int), c.stream);
-  const size_t sm_s = enc_smem(false), sm_g = enc_smem(true);
-  cudaFuncSetAttribute((const void*)k_codec_encode<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s);
-  cudaFuncSetAttribute((const void*)k_codec_encode<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s);
-  k_codec_encode<false, false><<<(unsigned)nch, SN_T, sm_s, c.stream>>>(d_boxes, n, nullptr, 0, nullptr, nullptr, d_rsize,
-                                                                        nullptr, nullptr, d_ovf + 1, d_ovf, c.st);
+  int* d_ovf = M.get<int>(nch + 1);  // count, then the chunks that need global tables
+  unsigned* d_rank = M.get<unsigned>((size_t)2 * n);
+  if (!d_rsize || !d_roff || !d_ovf || !d_rank) return gbi::set_err(ctx, GB_ERR_OOM, "snap encode scratch");
+  cudaMemsetAsync(d_ovf, 0, (nch + 1) * sizeof(int), c.stream);
+  const size_t sm_s = rank_smem(false), sm_g = rank_smem(true);
+  cudaFuncSetAttribute((const void*)k_enc_rank<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_s);
+  k_enc_rank<false><<<(unsigned)nch, SN_T, sm_s, c.stream>>>(d_boxes, n, nullptr, 0, nullptr, d_rank, d_ovf + 1, d_ovf,
+                                                             c.st);
   ++c.launches;
   int novf = 0;
   cudaMemcpyAsync(&novf, d_ovf, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
-  if (cudaStreamSynchronize(c.stream) != cudaSuccess) return gbi::set_err(ctx, GB_ERR_CUDA, "snap encode (size)");
-  unsigned long long* gkeys = nullptr;
-  unsigned* gpos = nullptr;
-  int gblocks = 0;
+  if (cudaStreamSynchronize(c.stream) != cudaSuccess) return gbi::set_err(ctx, GB_ERR_CUDA, "snap encode (ranks)");
   if (novf) {
-    gblocks = std::min(novf, std::max(1, c.nsm));
-    gkeys = M.get<unsigned long long>((size_t)gblocks * 2 * (1 << SN_GTAB_LOG));
-    gpos = M.get<unsigned>((size_t)gblocks * 2 * (1 << SN_GTAB_LOG));
-    if (!gkeys || !gpos) return gbi::set_err(ctx, GB_ERR_OOM, "snap encode tables");
-    k_codec_encode<true, false><<<gblocks, SN_T, sm_g, c.stream>>>(d_boxes, n, d_ovf + 1, novf, gkeys, gpos, d_rsize,
-                                                                   nullptr, nullptr, nullptr, nullptr, c.st);
+    const int gblocks = std::min(novf, std::max(1, c.nsm));
+    unsigned long long* gtab = M.get<unsigned long long>((size_t)gblocks * SN_GTAB_SLOTS);
+    if (!gtab) return gbi::set_err(ctx, GB_ERR_OOM, "snap encode tables");
+    k_enc_rank<true><<<gblocks, SN_T, sm_g, c.stream>>>(d_boxes, n, d_ovf + 1, novf, gtab, d_rank, nullptr, nullptr,
+                                                        c.st);
     ++c.launches;
   }
+  k_enc_emit<false><<<(unsigned)nch, SN_T, 0, c.stream>>>(d_boxes, n, d_rank, d_rsize, nullptr, nullptr, c.st);
+  ++c.launches;
   std::vector<long long> rsize(nch), roff(nch + 1, 0);
   cudaMemcpyAsync(rsize.data(), d_rsize, nch * 8, cudaMemcpyDeviceToHost, c.stream);
   if (cudaStreamSynchronize(c.stream) != cudaSuccess) return gbi::set_err(ctx, GB_ERR_CUDA, "snap encode (size)");
@@ -921,15 +978,8 @@ int snap_encode(gb_context* ctx, const int4* d_boxes, long long n, int method, u
   if (method != 0 && !d_raw) return gbi::set_err(ctx, GB_ERR_OOM, "snap raw buffer");
   unsigned char* rawbuf = method == 0 ? d_out : d_raw;
   cudaMemcpyAsync(d_roff, roff.data(), (nch + 1) * 8, cudaMemcpyHostToDevice, c.stream);
-  k_codec_encode<false, true><<<(unsigned)nch, SN_T, sm_s, c.stream>>>(d_boxes, n, nullptr, 0, nullptr, nullptr, nullptr,
-                                                                       d_roff, rawbuf, d_ovf + nch + 2, d_ovf + nch + 1,
-                                                                       c.st);
+  k_enc_emit<true><<<(unsigned)nch, SN_T, 0, c.stream>>>(d_boxes, n, d_rank, nullptr, d_roff, rawbuf, c.st);
   ++c.launches;
-  if (novf) {
-    k_codec_encode<true, true><<<gblocks, SN_T, sm_g, c.stream>>>(d_boxes, n, d_ovf + 1, novf, gkeys, gpos, nullptr,
-                                                                  d_roff, rawbuf, nullptr, nullptr, c.st);
-    ++c.launches;
-  }
   if (method == 0) {
     for (long long i = 0; i < nch; ++i) {
       meta[3 * i] = std::min((long long)SN_CHUNK, n - i * SN_CHUNK);
@@ -959,8 +1009,8 @@ int snap_encode(gb_context* ctx, const int4* d_boxes, long long n, int method, u
   if (nfrag) {
     cudaMemcpyAsync(d_fsrc, fsrc.data(), nfrag * 8, cudaMemcpyHostToDevice, c.stream);
     cudaMemcpyAsync(d_flen, flen.data(), nfrag * 4, cudaMemcpyHostToDevice, c.stream);
-    cudaFuncSetAttribute((const void*)k_snappy_compress, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 4096 * 4);
-    k_snappy_compress<<<(unsigned)((nfrag + 3) / 4), 128, 4 * 4096 * 4, c.stream>>>(d_raw, d_fsrc, d_flen, nfrag, d_fout,
+    cudaFuncSetAttribute((const void*)k_snappy_compress, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 4096 * 2);
+    k_snappy_compress<<<(unsigned)((nfrag + 7) / 8), 256, 8 * 4096 * 2, c.stream>>>(d_raw, d_fsrc, d_flen, nfrag, d_fout,
                                                                                     d_flout, c.st);
     ++c.launches;
   }
@@ -1033,12 +1083,14 @@ int snap_decode(gb_context* ctx, const unsigned char* d_data, const long long* m
   const long long* d_clen = d_tab + 3 * (nch + 1);
   const unsigned char* raw = d_data;
   if (method != 0) {
-    k_snappy_decompress<<<(unsigned)((nch + 3) / 4), 128, 0, c.stream>>>(d_data, d_coff, d_clen, d_raw, d_roff, d_rlen,
-                                                                         nch, c.st);
+    cudaFuncSetAttribute((const void*)k_snappy_decompress, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         SN_RING + SN_STAGE);
+    k_snappy_decompress<<<(unsigned)nch, 32, SN_RING + SN_STAGE, c.stream>>>(d_data, d_coff, d_clen, d_raw, d_roff,
+                                                                             d_rlen, nch, c.st);
     ++c.launches;
     raw = d_raw;
   }
-  k_codec_bounds<<<(unsigned)((nch + 3) / 4), 128, 0, c.stream>>>(raw, d_roff, d_rlen, n, nch, d_rec, c.st);
+  k_codec_bounds<<<(unsigned)nch, SN_BT, 0, c.stream>>>(raw, d_roff, d_rlen, n, nch, d_rec, c.st);
   k_codec_decode<<<(unsigned)nch, SN_T, 0, c.stream>>>(raw, d_roff, d_rec, n, d_dict, d_boxes, c.st);
   c.launches += 2;
   return gb_sync(ctx, nullptr);
