@@ -427,6 +427,7 @@ def main():
     ap.add_argument("--sort-n", type=int, default=200_000_000)
     ap.add_argument("--no-sort", action="store_true")
     ap.add_argument("--sort-no-tune", action="store_true", help="time the default sort plan only")
+    ap.add_argument("--grid", default="auto", help="tile grid log2 (slab height) of the deck, or 'auto' to tune")
     ap.add_argument("--snap-only", action="store_true")
     ap.add_argument("--no-snap", action="store_true")
     ap.add_argument("--snap-n", type=int, default=10_000_000, help="boxes per stdcell layer of the SNAP leg")
@@ -463,6 +464,12 @@ def main():
     ctx.set_stream(stream.cuda_stream)
     P = ctx.layer(boxes, off)
     ctx.sync()
+    grid_ms = None
+    if args.grid == "auto":  # slab height (tile grid) picked by the autotuner, outside the timed region
+        grid, grid_ms = ctx.grid_autotune(P, 1)
+    else:
+        grid = int(args.grid)
+        ctx.set_grid(grid)
 
     # ---- capture the batched chain once (OP1 + union area), profiling events inside
     mark = ctx.mark()
@@ -526,7 +533,7 @@ def main():
         import oracle as O
         O.build()
         ks = sample_cells(off, 400_000)
-        ec, ea = O.op1_cells(boxes[:off[ks]], off[:ks + 1])
+        ec, ea = O.op1_cells(boxes[:off[ks]], off[:ks + 1], grid_log2=grid)
         torch.cuda.synchronize()
         area_dev = area_t[:ks].cpu().numpy()  # as written by the last timed graph replay
         ok = np.array_equal(counts[:ks], ec) and np.array_equal(area_dev, ea)
@@ -588,7 +595,7 @@ def main():
         "config": {"workload": "OP1 deck (GROW 1, SIZE -1, 2x FRAME-NOT, 2x AND, 2x ASSERT_ZERO) + Klee "
                                "union area on %d cells, lognormal box counts (median %d, sigma 0.92, "
                                "clip 100..200000), cfg0-style cells" % (args.cells, args.median),
-                   "cells": args.cells, "boxes": nbox, "grid_log2": 16, "seed": args.seed,
+                   "cells": args.cells, "boxes": nbox, "grid_log2": grid, "grid_tuning_ms": grid_ms, "seed": args.seed,
                    "form": "batched: one CUDA-graph replay of persistent kernels per step",
                    "l2": "inputs (%d MB) larger than L2; no flush" % (nbox * 16 // 2**20)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

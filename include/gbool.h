@@ -343,6 +343,18 @@ int gb_snap_file_info(const char* path, long long* total_boxes, long long* num_c
 int gb_restore_snap_to_layer(gb_context* ctx, const char* path, c_box* d_boxes, long long cap, long long* n,
                              long long* pnum);
 
+/* Tile grid of the operators on this context: slab height 2^g dbu,
+ * 10 <= g <= 16 (default 16).  Results on two grids hold the same point set
+ * and differ only in where strips are cut at tile edges. */
+int gb_set_grid(gb_context* ctx, int g);
+int gb_get_grid(gb_context* ctx);
+/* Slab-height autotuner: runs the OP1 chain with the union area
+ * (gb_op1_area) on P with amount a once untimed and once timed at each grid
+ * g = 13..16 and leaves the fastest set on the context (*best_g).  ms_out
+ * (4 floats, may be NULL) receives the times in ms, -1 for a grid that did
+ * not run.  Synchronous. */
+int gb_grid_autotune(gb_context* ctx, gb_layer* P, int32_t a, int* best_g, float* ms_out);
+
 /* CUDA-graph capture of an operator chain on the context stream.  Every
  * replay restarts the work arena at the offset it had at gb_graph_begin. */
 typedef struct gb_graph gb_graph;

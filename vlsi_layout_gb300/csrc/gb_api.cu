@@ -66,13 +66,15 @@ void drop_layer(gb_context* ctx, gb_layer* L) {
   L->own_boxes = L->own_coff = L->own_cell = nullptr;
 }
 
+// The binned form of L on grid g: L itself, the cached binning of a raw
+// layer, or a new binning (from raw boxes or from a result on another grid).
 gb_layer* binned_of(gb_context* ctx, gb_layer* L, int g) {
-  if (L->binned) return L;
-  if (L->bin_cache && !L->bin_cache->dead) return L->bin_cache;
+  if (L->binned && L->g == g) return L;
+  if (!L->binned && L->bin_cache && !L->bin_cache->dead && L->bin_cache->g == g) return L->bin_cache;
   gb_layer* B = new_arena_layer(ctx, L->ncell, g);
   if (!B) return nullptr;
-  gb_launch_rebin(ctx->c, L->d, 0, B->d, L->ncell, g, 0, 0, 0, 0);
-  L->bin_cache = B;
+  gb_launch_rebin(ctx->c, L->d, L->binned, B->d, L->ncell, g, 0, 0, 0, 0);
+  if (!L->binned) L->bin_cache = B;
   return B;
 }
 
@@ -397,6 +399,14 @@ extern "C" int gb_arena_release(gb_context* ctx, unsigned long long mark) {
   return GB_OK;
 }
 
+extern "C" int gb_set_grid(gb_context* ctx, int g) {
+  if (!ctx || g < 10 || g > 16) return GB_ERR_ARG;
+  ctx->c.grid = g;
+  return GB_OK;
+}
+
+extern "C" int gb_get_grid(gb_context* ctx) { return ctx ? ctx->c.grid : -1; }
+
 extern "C" int gb_set_capacity_factor(gb_context* ctx, int factor) {
   if (!ctx || factor < 1) return GB_ERR_ARG;
   ctx->c.cap_factor = factor;
@@ -556,7 +566,7 @@ extern "C" void gb_layer_free(gb_context* ctx, gb_layer* L) {
 // ======================================================================= operators
 gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode) {
   GbCtx& c = ctx->c;
-  const int g = 16;
+  const int g = c.grid;
   gb_layer* Ab = binned_of(ctx, A, g);
   const bool single = op == GB_OP_MERGE || op == GB_OP_OVERLAP;
   gb_layer* Bb = (B && !single) ? binned_of(ctx, B, g) : nullptr;
@@ -581,7 +591,7 @@ extern "C" int gb_op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, gb_
 }
 
 gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge) {
-  const int g = 16;
+  const int g = ctx->c.grid;
   gb_layer* R = new_arena_layer(ctx, A->ncell, g);
   if (!R) return nullptr;
   gb_launch_rebin(ctx->c, A->d, A->binned, R->d, A->ncell, g, E, N, W, S);
@@ -599,7 +609,7 @@ extern "C" int gb_op_grow(gb_context* ctx, gb_layer* A, int32_t E, int32_t N, in
 // SIZE(-t): R = P - ((F - P) (+) [-t,t]^2), F = cell bbox grown by t.
 gb_layer* op_erode(gb_context* ctx, gb_layer* P, int t, gb_layer** frame_out, gb_layer** comp_out) {
   GbCtx& c = ctx->c;
-  const int g = 16;
+  const int g = c.grid;
   gb_layer* Pb = binned_of(ctx, P, g);
   if (!Pb) return nullptr;
   gb_layer* F = new_arena_layer(ctx, P->ncell, g);

@@ -18,6 +18,8 @@
 #include "gbool.h"
 #include "gb_internal.h"
 
+#define GB_GRID_TUNE_MIN 13  // smallest tile grid (log2 dbu) the slab-height tuner tries
+
 using namespace gbi;
 
 struct gb_graph {
@@ -259,6 +261,54 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
   cudaFree(dl);
   gb_layer_free(ctx, P);
   return e;
+}
+
+// Slab height of the operators: the OP1 chain with the union area runs on P
+// once untimed and once timed (CUDA events on the context stream) at each
+// tile grid 2^13 .. 2^16 dbu, and the fastest grid stays set on the context.
+// Results differ between grids only in where strips are cut (the point sets
+// are the same).  ms_out (4 entries, may be NULL): the times, -1 for a grid
+// that did not run.
+extern "C" int gb_grid_autotune(gb_context* ctx, gb_layer* P, int32_t a, int* best_g, float* ms_out) {
+  if (!ctx || !P || P->dead || !best_g) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  long long* d_area = nullptr;
+  if (cudaMalloc(&d_area, (size_t)P->ncell * 8) != cudaSuccess) return set_err(ctx, GB_ERR_OOM, "grid tuning buffer");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int old = c.grid;
+  float best = 0.f;
+  int bg = -1;
+  for (int g = GB_GRID_TUNE_MIN; g <= 16; ++g) {
+    c.grid = g;
+    float ms = -1.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      const int r = gb_run_retry(ctx, [&]() -> int {
+        gb_layer* outs[6];
+        cudaEventRecord(e0, c.stream);
+        const int q = gb_op1_area(ctx, P, a, outs, d_area);
+        cudaEventRecord(e1, c.stream);
+        return q;
+      });
+      if (r) {
+        ms = -1.f;
+        break;
+      }
+      if (rep) cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (ms_out) ms_out[g - GB_GRID_TUNE_MIN] = ms;
+    if (ms > 0.f && (bg < 0 || ms < best)) {
+      best = ms;
+      bg = g;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d_area);
+  c.grid = bg < 0 ? old : bg;
+  *best_g = c.grid;
+  return bg < 0 ? set_err(ctx, GB_ERR_CAPACITY, "the deck ran on no grid") : GB_OK;
 }
 
 extern "C" int gb_debug_lookback_timeout(gb_context* ctx, int spin_limit) {

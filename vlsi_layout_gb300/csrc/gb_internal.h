@@ -42,6 +42,7 @@ struct GbCtx {
   bool timing = false;               // per-phase clock64 counters in the tile kernel
   long long launches = 0;            // kernels issued by the engine (host-side count)
   void* rs = nullptr;                // radix sort state (histograms, look-back status), gb_radix.cu
+  int grid = 16;                     // tile grid log2 (slab height 2^grid dbu) of the operators
 };
 
 struct gb_layer {

@@ -111,6 +111,9 @@ def lib():
         "gb_serve_result_boxes": (ctypes.c_int, [P, ctypes.c_int, P, u64, P]),
         "gb_serve_destroy": (None, [P]),
         "gb_bool_tile_noalloc": (ctypes.c_int, [ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, P, i64, P, P, P]),
+        "gb_set_grid": (ctypes.c_int, [P, ctypes.c_int]),
+        "gb_get_grid": (ctypes.c_int, [P]),
+        "gb_grid_autotune": (ctypes.c_int, [P, P, i32, P, P]),
         "gb_snap_max_bytes": (ctypes.c_int, [i64, P]),
         "gb_compress_boxes_to_stream": (ctypes.c_int, [P, P, i64, ctypes.c_int, P, i64, P, P]),
         "gb_decompress_stream_to_boxes": (ctypes.c_int, [P, P, P, i64, ctypes.c_int, P]),
@@ -197,6 +200,22 @@ class Context:
 
     def set_stream(self, stream_handle):
         self._chk(lib().gb_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def set_grid(self, g):
+        """Tile grid of the operators: slab height 2^g dbu (10..16, default 16)."""
+        self._chk(lib().gb_set_grid(self.h, g))
+
+    @property
+    def grid(self):
+        return lib().gb_get_grid(self.h)
+
+    def grid_autotune(self, P, amount=1):
+        """Time the OP1 deck on layer P at tile grids 2^13..2^16 and keep the
+        fastest on the context.  Returns (grid, {grid: ms or None})."""
+        g = ctypes.c_int()
+        ms = (ctypes.c_float * 4)()
+        self._chk(lib().gb_grid_autotune(self.h, P.h, amount, ctypes.byref(g), ms))
+        return g.value, {13 + i: (ms[i] if ms[i] > 0 else None) for i in range(4)}
 
     def mark(self):
         return lib().gb_arena_mark(self.h)
