@@ -26,11 +26,11 @@
 // it is at least 8 bytes long, emits Snappy literal / copy elements.  Fragments are concatenated behind the
 // chunk's length preamble.  Decoding takes one warp per chunk through the
 // elements (all element forms of the format are accepted), with the last
-// 64 KB of output in a shared-memory ring for the copies.
-// Decoding the codec: one CTA per chunk finds the record boundaries (all
-// threads compute the length a record would have at each byte of a 4 KB
-// window, and the lengths of the next four records from there; one thread
-// walks the chain four records per load), then one CTA per chunk parses the
+// 32 KB of output in a shared-memory ring for the copies.
+// Decoding the codec: one CTA per chunk finds the record boundaries (seven
+// warps compute, per 4 KB window, the lengths of the next four records from
+// every byte; one thread walks the chain four records per load, overlapped
+// with the next window's computation), then one CTA per chunk parses the
 // records 1024 at a time, rebuilds the anchors and dictionary indices with
 // block scans and gathers widths and heights from per-chunk dictionaries.
 #include <cstdio>
@@ -401,33 +401,46 @@ k_enc_emit(const int4* __restrict__ boxes, long long n, const unsigned* __restri
 }
 
 // ---------------------------------------------------------------- codec decoder
-// length of the record starting at p (p[0..40] readable), 0 when malformed
-__device__ __forceinline__ int sn_rec_len(const unsigned char* p) {
-  const unsigned info = p[0];
+// One 256-thread CTA per chunk: rec[c * SN_CHUNK + r] = offset of record r in
+// the chunk.  The chunk is taken in 4 KB windows.  For a window, warps 1..7
+// load its bytes (and the look-ahead), mark the varint continuation bits
+// with ballots, compute at every byte the length a record starting there
+// would have (each varint's length is one find-first-zero in the continuation
+// bits) and then, per byte, the lengths of the four records of the chain
+// starting there (one word).  Meanwhile lane 0 of warp 0 walks the previous
+// window's chain four records per shared-memory load.
+#define SN_BT 256
+#define SN_BWIN 4096
+#define SN_BPAD 256  // lengths are needed up to three records (3 * 41 bytes) past the window
+#define SN_BBUF (SN_BWIN + SN_BPAD + 64)
+__device__ __forceinline__ int sn_vl(const unsigned* cont, int q) {  // varint length at q (0: longer than 10)
+  const unsigned long long w = ((unsigned long long)cont[(q >> 5) + 1] << 32) | cont[q >> 5];
+  const int k = __ffsll(~(w >> (q & 31)));  // first byte without the continuation bit, 1-based
+  return k <= 10 ? k : 0;
+}
+
+__device__ __forceinline__ int sn_rec_len_bits(const unsigned char* buf, const unsigned* cont, int b) {
+  const unsigned info = buf[b];
   int l = 1, k;
   if (info & 32) {
-    sn_get_varint(p + l, &k);
-    if (!k) return 0;
+    if (!(k = sn_vl(cont, b + l))) return 0;
     l += k;
   }
   if (info & 64) {
-    sn_get_varint(p + l, &k);
-    if (!k) return 0;
+    if (!(k = sn_vl(cont, b + l))) return 0;
     l += k;
   }
   if (info & 1) {
     if (info & 2) {
-      sn_get_varint(p + l, &k);
-      if (!k) return 0;
+      if (!(k = sn_vl(cont, b + l))) return 0;
       l += k;
     } else {
       l += 2;
     }
   }
-  if (!(info & 16) && (info & 4)) {
+  if ((info & 20) == 4) {
     if (info & 8) {
-      sn_get_varint(p + l, &k);
-      if (!k) return 0;
+      if (!(k = sn_vl(cont, b + l))) return 0;
       l += k;
     } else {
       l += 2;
@@ -436,83 +449,105 @@ __device__ __forceinline__ int sn_rec_len(const unsigned char* p) {
   return l;
 }
 
-// One 256-thread CTA per chunk: rec[c * SN_CHUNK + r] = offset of record r in
-// the chunk.  Per 4 KB window every thread computes the length a record
-// would have at each of its bytes, then, per byte, the lengths of the four
-// records a chain starting there would have (one word); thread 0 walks the
-// chain four records per shared-memory load.
-#define SN_BT 256
-#define SN_BWIN 4096
-#define SN_BPAD 256  // lengths are needed up to three records (3 * 41 bytes) past the window
 __global__ void __launch_bounds__(SN_BT)
 k_codec_bounds(const unsigned char* __restrict__ raw, const long long* __restrict__ raw_off,
                const long long* __restrict__ raw_len, long long n, long long nchunks, unsigned* __restrict__ rec,
                DStatus* st) {
-  __shared__ unsigned char buf[SN_BWIN + SN_BPAD + SN_WPAD];
+  __shared__ unsigned char buf[SN_BBUF];
+  __shared__ unsigned cont[SN_BBUF / 32 + 2];
   __shared__ unsigned char lenb[SN_BWIN + SN_BPAD];
-  __shared__ unsigned quad[SN_BWIN];
-  __shared__ long long s_pos;
-  __shared__ int s_r, s_bad, s_skip;
-  const int t = threadIdx.x;
+  __shared__ unsigned quad[2][SN_BWIN];
+  __shared__ int s_pos, s_r, s_bad, s_skip;  // s_pos: offset into the next window
+  const int t = threadIdx.x, wid = t >> 5;
   const long long c = blockIdx.x;
-  if (t == 0) s_skip = *(volatile int*)&st->err;  // the Snappy layer was malformed: one read for the whole CTA
+  if (t == 0) {
+    s_skip = *(volatile int*)&st->err;  // the Snappy layer was malformed: one read for the whole CTA
+    s_pos = 0;
+    s_r = 0;
+    s_bad = 0;
+  }
   __syncthreads();
   if (s_skip) return;
   const int nb = (int)min((long long)SN_CHUNK, n - c * SN_CHUNK);
   const long long L = raw_len[c];
   const unsigned char* base = raw + raw_off[c];
   unsigned* out = rec + c * SN_CHUNK;
-  long long pos = 0;
-  int r = 0, bad = 0;
-  for (long long ws = 0; r < nb && !bad; ws += SN_BWIN) {
-    if (ws >= L) {
-      bad = 1;
+  auto sync = [&](int bar, int nt) {
+    if (bar)
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nt) : "memory");
+    else
+      __syncthreads();
+  };
+  // quads of window w into quad[w & 1]; run by threads [t0, t0 + nt) (whole warps), barrier id bar
+  auto build = [&](long long w, int t0, int nt, int bar) {
+    const long long ws = w * SN_BWIN;
+    const int u = t - t0;
+#pragma unroll 8
+    for (int b = u; b < SN_BBUF; b += nt) buf[b] = ws + b < L ? base[ws + b] : 0;  // independent loads in flight
+    sync(bar, nt);
+    for (int b = u; b < SN_BBUF; b += nt) {
+      const unsigned m = __ballot_sync(0xffffffffu, buf[b] & 128u);
+      if ((b & 31) == 0) cont[b >> 5] = m;
+    }
+    if (u < 2) cont[SN_BBUF / 32 + u] = 0xffffffffu;  // past the buffer: a varint there is too long
+    sync(bar, nt);
+    for (int b = u; b < SN_BWIN + SN_BPAD; b += nt) lenb[b] = (unsigned char)sn_rec_len_bits(buf, cont, b);
+    sync(bar, nt);
+    unsigned* qd = quad[w & 1];
+    for (int b = u; b < SN_BWIN; b += nt) {
+      const unsigned l0 = lenb[b];
+      const unsigned l1 = l0 ? lenb[b + l0] : 0u;
+      const unsigned l2 = l1 ? lenb[b + l0 + l1] : 0u;
+      const unsigned l3 = l2 ? lenb[b + l0 + l1 + l2] : 0u;
+      qd[b] = l0 | (l1 << 8) | (l2 << 16) | (l3 << 24);
+    }
+  };
+  const long long nwin = (L + SN_BWIN - 1) / SN_BWIN;
+  if (nwin > 0) build(0, 0, SN_BT, 0);
+  __syncthreads();
+  for (long long w = 0;; ++w) {
+    // every thread reads the walk's state before the barrier; lane 0 of warp 0 changes it only after
+    const int done = (s_r >= nb || s_bad) ? 1 : (w >= nwin ? 2 : 0);
+    __syncthreads();
+    if (done) {
+      if (done == 2 && t == 0) s_bad = 1;  // the stream ends before the chunk's last record
       break;
     }
-#pragma unroll 4
-    for (int b = t; b < SN_BWIN + SN_BPAD + SN_WPAD; b += SN_BT) buf[b] = ws + b < L ? base[ws + b] : 0;
-    __syncthreads();
-    for (int b = t; b < SN_BWIN + SN_BPAD; b += SN_BT) lenb[b] = (unsigned char)sn_rec_len(&buf[b]);
-    __syncthreads();
-    for (int b = t; b < SN_BWIN; b += SN_BT) {
-      unsigned q = 0;
-      int at = b;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned l = at < SN_BWIN + SN_BPAD ? lenb[at] : 0u;
-        q |= l << (8 * k);
-        if (!l) break;
-        at += (int)l;
-      }
-      quad[b] = q;
-    }
-    __syncthreads();
     if (t == 0) {
-      while (r < nb && pos < ws + SN_BWIN && !bad) {
-        const unsigned q = quad[pos - ws];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (r >= nb || pos >= ws + SN_BWIN) break;  // later records are found from the next window
-          const unsigned l = (q >> (8 * k)) & 255u;
-          if (pos >= L || !l) {
-            bad = 1;
-            break;
-          }
-          out[r++] = (unsigned)pos;
-          pos += l;
+      const unsigned ws = (unsigned)(w * SN_BWIN);
+      const unsigned* qd = quad[w & 1];
+      const int lim = (int)min((long long)SN_BWIN, L - (long long)ws);  // starts inside window and stream
+      int pos = s_pos, r = s_r, bad = 0;
+      while (r < nb && pos < SN_BWIN) {
+        const unsigned q = qd[pos];
+        const int l0 = q & 255u, l1 = (q >> 8) & 255u, l2 = (q >> 16) & 255u, l3 = q >> 24;
+        const int p1 = pos + l0, p2 = p1 + l1, p3 = p2 + l2;
+        if (l3 && p3 < lim && r + 4 <= nb) {  // four whole records (l3 != 0 implies l0..l2 != 0)
+          out[r] = ws + pos;
+          out[r + 1] = ws + p1;
+          out[r + 2] = ws + p2;
+          out[r + 3] = ws + p3;
+          r += 4;
+          pos = p3 + l3;
+          continue;
         }
+        if (pos >= lim || !l0) {  // the stream ends early, or a malformed record
+          bad = 1;
+          break;
+        }
+        out[r++] = ws + pos;
+        pos = p1;
       }
-      s_pos = pos;
+      if (!bad && r >= nb && (long long)ws + pos > L) bad = 1;  // the last record runs past the stream
+      s_pos = pos - SN_BWIN;
       s_r = r;
       s_bad = bad;
+    } else if (wid > 0 && w + 1 < nwin) {
+      build(w + 1, 32, SN_BT - 32, 1);
     }
     __syncthreads();
-    pos = s_pos;
-    r = s_r;
-    bad = s_bad;
-    __syncthreads();
   }
-  if (t == 0 && (bad || pos > L)) gb_set_error(st, GB_ERR_CORRUPT, KID_SNAP_BOUNDS, c);
+  if (t == 0 && s_bad) gb_set_error(st, GB_ERR_CORRUPT, KID_SNAP_BOUNDS, c);
 }
 
 // One CTA per chunk: records -> boxes.  dict: per chunk 2 * SN_CHUNK ints.
@@ -672,7 +707,9 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
     __syncwarp();
     if (has && (peers >> lane) == 1u) tab[h] = (unsigned short)(q + 1);
     __syncwarp();
-    const bool ok = has && cand && sn_ld32(src + cand - 1) == v;
+    // a candidate counts when its first 8 bytes match (shorter copies are not emitted)
+    const bool has8 = q + SN_MIN_MATCH <= fl;
+    const bool ok = has8 && cand && sn_ld32(src + cand - 1) == v && sn_ld32(src + cand + 3) == sn_ld32(src + q + 4);
     const unsigned okm = __ballot_sync(0xffffffffu, ok);
     while (p < bb + 32 && p + 4 <= fl) {
       const unsigned m = okm & (0xffffffffu << (p - bb));
@@ -683,7 +720,7 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
       const int ln = __ffs(m) - 1;
       p = bb + ln;
       const int qs = (int)__shfl_sync(0xffffffffu, cand, ln) - 1;
-      int L = 4;
+      int L = SN_MIN_MATCH;
       for (;;) {
         const int a = p + L + lane;
         const bool eq = a < fl && src[qs + L + lane] == src[a];
@@ -693,10 +730,6 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
           break;
         }
         L += 32;
-      }
-      if (L < SN_MIN_MATCH) {  // too short to pay for an element: literal byte
-        p += 1;
-        continue;
       }
       // pending literal
       if (p > lit) {
@@ -773,15 +806,16 @@ __global__ void k_snappy_gather(const unsigned char* __restrict__ fout, const in
 // One single-warp CTA per chunk: Snappy raw stream -> codec bytes.  The
 // element tags are read from a 4 KB staging copy of the input, literals are
 // copied with four loads in flight per lane, and copies whose source lies in
-// the last 64 KB of output are read from a shared-memory ring of it.
-#define SN_RING 65536
+// the last 32 KB of output are read from a shared-memory ring of it (older
+// sources from global memory).
+#define SN_RING 32768
 #define SN_STAGE 4096
 __global__ void __launch_bounds__(32)
 k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* __restrict__ in_off,
                     const long long* __restrict__ in_len, unsigned char* out_all, const long long* __restrict__ out_off,
                     const long long* __restrict__ out_len, long long nchunks, DStatus* st) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  unsigned char* ring = dsm;           // output byte x at ring[x % SN_RING]
+  unsigned char* ring = dsm;           // output byte x at ring[x % SN_RING] for the last SN_RING bytes
   unsigned char* stg = dsm + SN_RING;  // input bytes [sb, sb + SN_STAGE)
   const int lane = threadIdx.x;
   const long long c = blockIdx.x;
@@ -795,8 +829,8 @@ k_snappy_decompress(const unsigned char* __restrict__ in_all, const long long* _
     if (p < sb || p + 8 > sb + SN_STAGE) {
       sb = p;
       __syncwarp();
-#pragma unroll 4
-      for (int i = lane; i < SN_STAGE; i += 32) stg[i] = sb + i < len ? in[sb + i] : 0;
+#pragma unroll 16
+      for (int i = lane; i < SN_STAGE; i += 32) stg[i] = sb + i < len ? in[sb + i] : 0;  // 16 loads in flight
       __syncwarp();
     }
   };
