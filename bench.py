@@ -406,6 +406,65 @@ def snap_leg(n_per=10_000_000, steps=3, cpu_chunks=96):
     return res
 
 
+def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
+    """PNUM connectivity (PerformMerge: closed-overlap union-find, labels
+    1..R by smallest index) and the overlap statistics (strict pairs,
+    singletons: ComputeInteractions / FindSingletons) of one standard-cell
+    layout (4 layers x n_per boxes + 2% contacts that join them, in a die
+    sized for ~6.7% singletons), through the host API (H2D of the boxes and
+    D2H of labels / mask inside the timed region), then the oracle
+    (single-threaded, as the reference's sequential union-find) on the same
+    generator at 1/cpu_scale of the boxes and the same density."""
+    import torch
+    from vlsi_layout_gb300 import engine
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import gen
+    def layout(m):
+        sc = gen.stdcell_layers(m, die=int(400_000 * (m / 100_000) ** 0.5), seed=4)
+        return np.concatenate([sc[k] for k in ("poly", "met1", "met2", "li1", "contact")])
+    B = layout(n_per)
+    n = len(B)
+    res = {"n": n, "workload": "stdcell layers (poly, met1, met2, li1 x %d + 2%% contacts, die %d dbu) as one "
+           "layer" % (n_per, int(400_000 * (n_per / 100_000) ** 0.5))}
+    with engine.Context(0) as ctx:
+        tc, ti = [], []
+        ncomp = pairs = singles = None
+        for it in range(steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ncomp, labels = ctx.components(B)
+            t1 = time.perf_counter()
+            pairs, singles, _ = ctx.interactions(B)
+            t2 = time.perf_counter()
+            if it:
+                tc.append(t1 - t0)
+                ti.append(t2 - t1)
+    sc_, si_ = statistics.median(tc), statistics.median(ti)
+    res.update({"components": int(ncomp), "strict_pairs": int(pairs), "singletons": int(singles),
+                "components_s": sc_, "components_boxes_per_s": n / sc_,
+                "interactions_s": si_, "interactions_boxes_per_s": n / si_,
+                "timing": "host wall clock around gb_components / gb_interactions (host boxes in, labels / mask out)"})
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    S = layout(n_per // cpu_scale)
+    t0 = time.perf_counter()
+    en, elab = O.components(S)
+    t1 = time.perf_counter()
+    ep, es, emask = O.interactions(S)
+    t2 = time.perf_counter()
+    with engine.Context(0) as ctx:  # parity on the sample: labels, pair count, singleton mask
+        gn, glab = ctx.components(S)
+        gp, gs, gmask = ctx.interactions(S)
+    ok = gn == en and np.array_equal(glab, elab) and (gp, gs) == (ep, es) and np.array_equal(gmask, emask)
+    res["parity"] = "labels, strict pairs and singleton mask bit-exact on the %d-box sample: %s" % (
+        len(S), "pass" if ok else "FAIL")
+    res["cpu_baseline"] = {"components_boxes_per_s": len(S) / (t1 - t0),
+                           "interactions_boxes_per_s": len(S) / (t2 - t1), "cores": 1, "kind": "port",
+                           "sample": "the same generator with %d boxes (1/%d, same density)" % (len(S), cpu_scale)}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,6 +488,8 @@ def main():
     ap.add_argument("--sort-no-tune", action="store_true", help="time the default sort plan only")
     ap.add_argument("--grid", default="auto", help="tile grid log2 (slab height) of the deck, or 'auto' to tune")
     ap.add_argument("--snap-only", action="store_true")
+    ap.add_argument("--conn-only", action="store_true")
+    ap.add_argument("--no-conn", action="store_true")
     ap.add_argument("--no-snap", action="store_true")
     ap.add_argument("--snap-n", type=int, default=10_000_000, help="boxes per stdcell layer of the SNAP leg")
     args = ap.parse_args()
@@ -437,6 +498,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps, tune=not args.sort_no_tune)}), flush=True)
+        return
+    if args.conn_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"connectivity": connectivity_leg(steps=args.steps)}), flush=True)
         return
     if args.snap_only:
         import torch
@@ -587,6 +653,9 @@ def main():
     snap = None
     if rank == 0 and not args.no_snap:
         snap = snap_leg(n_per=args.snap_n, steps=3)
+    conn = None
+    if rank == 0 and not args.no_conn:
+        conn = connectivity_leg(steps=2)
     value = replica_value(world, nbox, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
@@ -616,6 +685,7 @@ def main():
         "serving": serving,
         "sort": sort,
         "snap": snap,
+        "connectivity": conn,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
