@@ -407,7 +407,7 @@ def snap_leg(n_per=10_000_000, steps=3, cpu_chunks=96):
 
 
 def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
-    """PNUM connectivity (PerformMerge: closed-overlap union-find, labels
+    """Klee's-measure union area (calculate_union_area_fast), PNUM connectivity (PerformMerge: closed-overlap union-find, labels
     1..R by smallest index) and the overlap statistics (strict pairs,
     singletons: ComputeInteractions / FindSingletons) of one standard-cell
     layout (4 layers x n_per boxes + 2% contacts that join them, in a die
@@ -427,6 +427,21 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
     res = {"n": n, "workload": "stdcell layers (poly, met1, met2, li1 x %d + 2%% contacts, die %d dbu) as one "
            "layer" % (n_per, int(400_000 * (n_per / 100_000) ** 0.5))}
     with engine.Context(0) as ctx:
+        # Klee's-measure area of the layout (one cell): binning + count-mode union on the device
+        L = ctx.layer(B)
+        ctx.sync()
+        ta = []
+        area = None
+        for it in range(steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m = ctx.mark()
+            area = int(ctx.area(L)[0])
+            ctx.release(m)
+            t1 = time.perf_counter()
+            if it:
+                ta.append(t1 - t0)
+        L.free()
         tc, ti = [], []
         ncomp = pairs = singles = None
         for it in range(steps + 1):
@@ -440,7 +455,8 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
                 tc.append(t1 - t0)
                 ti.append(t2 - t1)
     sc_, si_ = statistics.median(tc), statistics.median(ti)
-    res.update({"components": int(ncomp), "strict_pairs": int(pairs), "singletons": int(singles),
+    res.update({"union_area": area, "area_s": statistics.median(ta), "area_boxes_per_s": n / statistics.median(ta),
+                "components": int(ncomp), "strict_pairs": int(pairs), "singletons": int(singles),
                 "components_s": sc_, "components_boxes_per_s": n / sc_,
                 "interactions_s": si_, "interactions_boxes_per_s": n / si_,
                 "timing": "host wall clock around gb_components / gb_interactions (host boxes in, labels / mask out)"})
@@ -453,14 +469,20 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
     t1 = time.perf_counter()
     ep, es, emask = O.interactions(S)
     t2 = time.perf_counter()
-    with engine.Context(0) as ctx:  # parity on the sample: labels, pair count, singleton mask
+    ea = O.union_area(S)
+    t3 = time.perf_counter()
+    with engine.Context(0) as ctx:  # parity on the sample: labels, pair count, singleton mask, area
         gn, glab = ctx.components(S)
         gp, gs, gmask = ctx.interactions(S)
-    ok = gn == en and np.array_equal(glab, elab) and (gp, gs) == (ep, es) and np.array_equal(gmask, emask)
-    res["parity"] = "labels, strict pairs and singleton mask bit-exact on the %d-box sample: %s" % (
+        LS = ctx.layer(S)
+        ga = int(ctx.area(LS)[0])
+    ok = gn == en and np.array_equal(glab, elab) and (gp, gs) == (ep, es) and np.array_equal(gmask, emask) \
+        and ga == ea
+    res["parity"] = "labels, strict pairs, singleton mask and union area bit-exact on the %d-box sample: %s" % (
         len(S), "pass" if ok else "FAIL")
     res["cpu_baseline"] = {"components_boxes_per_s": len(S) / (t1 - t0),
-                           "interactions_boxes_per_s": len(S) / (t2 - t1), "cores": 1, "kind": "port",
+                           "interactions_boxes_per_s": len(S) / (t2 - t1),
+                           "area_boxes_per_s": len(S) / (t3 - t2), "cores": 1, "kind": "port",
                            "sample": "the same generator with %d boxes (1/%d, same density)" % (len(S), cpu_scale)}
     return res
 
