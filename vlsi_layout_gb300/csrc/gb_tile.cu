@@ -90,6 +90,7 @@ struct TileSmem {
     unsigned char dbuf[1];
   };
   int sbnext;                            // next sub-band to hand to a warp
+  unsigned long long mbar;               // completion of phase D's bulk copies (one phase per tile)
   long long tmp64[33];
   long long tile;
   const unsigned long long* pa;
@@ -148,6 +149,30 @@ __device__ __forceinline__ int bm_rank2(const unsigned* bits, const unsigned* pr
 }
 
 __device__ __forceinline__ unsigned long long vchg(unsigned long long r) { return (r ^ (r << 1)) & ~1ull; }
+
+// ---- bulk copies of phase D (global scratch -> shared memory, completing on an mbarrier)
+#define TK_SPIN_LIMIT (1 << 22)
+#define KID_TILE_COPY 22
+__device__ __forceinline__ unsigned tk_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void tk_bulk(void* dst, const void* src, unsigned bytes, unsigned mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tk_smem(dst)),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+// bounded wait for the given phase parity; false after `limit` polls
+__device__ __forceinline__ bool tk_wait(unsigned mbar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
 
 // Allocation in the lower half of the CTA's scratch (one thread calls it).
 // When a dense tile outgrows it, the allocation spills into the work arena
@@ -499,6 +524,12 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
   const bool timing = (mode & 4) != 0;
   mode &= 3;
   long long tA = 0, tB = 0, tC = 0, tD = 0, t0 = 0;
+  const unsigned mbar = tk_smem(&s.mbar);
+  unsigned mph = 0;  // parity of the mbarrier phase the next bulk copies complete
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   for (;;) {
     __syncthreads();
     if (tid == 0) {
@@ -713,6 +744,10 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         tile_subband(s, op, sb, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
       }
     }
+    // the bulk copies of phase D (async proxy) read the records written above and overwrite shared
+    // memory written in phases A-C (generic proxy)
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (timing) { const long long t1 = clock64(); tC += t1 - t0; t0 = t1; }
     // ---- D: stitch and emit.  Piece records, chain links and the x / y value
@@ -722,7 +757,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
                                  sizeof(s.mc) + sizeof(s.srow));
     const bool prs = (long long)NP * 20 <= DBYTES;
     const int xyoff = nsb <= TK_MDS ? TK_MD_INTS : 0;  // metadata occupies the front of the region
-    const bool xys = Nx + Ny + xyoff <= 2 * TK_WMAX + 2 * (TK_WMAX / 2 + 1);
+    const int nx4 = (Nx + 3) & ~3, ny4 = (Ny + 3) & ~3;  // tables start on 16-byte boundaries
+    const bool xys = nx4 + ny4 + xyoff <= 2 * TK_WMAX + 2 * (TK_WMAX / 2 + 1);
     if (tid == 0 && !s.err && !prs) s.succ = (int*)sc_up(s, base, half, (unsigned long long)NP * 4 + 4);
     __syncthreads();
     if (s.err) {
@@ -736,39 +772,34 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     PieceRec* PR = prs ? reinterpret_cast<PieceRec*>(s.dbuf) : nullptr;
     int* succ = prs ? reinterpret_cast<int*>(s.dbuf + (size_t)NP * 16) : s.succ;
     const int* Xv = xys ? s.xyv + xyoff : s.Xt;
-    const int* Yv = xys ? s.xyv + xyoff + Nx : s.Yt;
+    const int* Yv = xys ? s.xyv + xyoff + nx4 : s.Yt;
     // record of global piece q, which belongs to sub-band sb
     auto REC = [&](int sb, int q) -> PieceRec { return prs ? PR[q] : s.sbrec[sb][q - s.sbinfo[sb].x]; };
     const int wid = gb_warp(), lane = gb_lane();
-    if (prs)
-      for (int sb = wid; sb < nsb; sb += TK_NW) {
-        const int4 inf = s.sbinfo[sb];
-        const PieceRec* src = s.sbrec[sb];
-        constexpr int RD = 4;
-        for (int j0 = lane; j0 < inf.y; j0 += RD * 32) {
-          PieceRec r[RD];
-#pragma unroll
-          for (int u = 0; u < RD; ++u)
-            if (j0 + u * 32 < inf.y) r[u] = src[j0 + u * 32];
-#pragma unroll
-          for (int u = 0; u < RD; ++u)
-            if (j0 + u * 32 < inf.y) PR[inf.x + j0 + u * 32] = r[u];
+    // piece records of every sub-band and the x / y value tables into shared memory by bulk copies
+    // (all 16-byte aligned: records are 16 bytes, scratch allocations are rounded to 16 bytes)
+    if ((prs && NP > 0) || xys) {
+      if (tid == 0) {
+        const unsigned bytes = (prs ? (unsigned)NP * 16u : 0u) + (xys ? (unsigned)(nx4 + ny4) * 4u : 0u);
+        asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(mbar),
+                     "r"(bytes)
+                     : "memory");
+        if (xys) {
+          if (nx4) tk_bulk(s.xyv + xyoff, s.Xt, (unsigned)nx4 * 4u, mbar);
+          if (ny4) tk_bulk(s.xyv + xyoff + nx4, s.Yt, (unsigned)ny4 * 4u, mbar);
         }
       }
-    if (xys) {
-      const int* xt = s.Xt;
-      const int* yt = s.Yt;
-      constexpr int VD = 8;
-      for (int i0 = tid; i0 < Nx + Ny; i0 += VD * TK_NT) {
-        int v[VD];
-#pragma unroll
-        for (int u = 0; u < VD; ++u) {
-          const int i = i0 + u * TK_NT;
-          v[u] = i < Nx ? xt[i] : i < Nx + Ny ? yt[i - Nx] : 0;
+      if (prs && wid == 0)
+        for (int sb = lane; sb < nsb; sb += 32) {
+          const int4 inf = s.sbinfo[sb];
+          if (inf.y > 0) tk_bulk(PR + inf.x, s.sbrec[sb], (unsigned)inf.y * 16u, mbar);
         }
-#pragma unroll
-        for (int u = 0; u < VD; ++u)
-          if (i0 + u * TK_NT < Nx + Ny) s.xyv[xyoff + i0 + u * TK_NT] = v[u];
+      const bool ok = tk_wait(mbar, mph, TK_SPIN_LIMIT);
+      mph ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) gb_set_error(st, GB_ERR_TIMEOUT, KID_TILE_COPY, t);
+        tk_wait(mbar, mph ^ 1u, TK_SPIN_LIMIT);  // let copies in flight land before the CTA exits
+        return;
       }
     }
     for (int p = tid; p < NP; p += TK_NT) succ[p] = -1;
