@@ -531,6 +531,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (;;) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // before this tile's bulk copies
     __syncthreads();
     if (tid == 0) {
       s.st = st;
@@ -572,11 +573,56 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     if (timing) t0 = clock64();
     // ---- A: tile ranks
-    for (int w = tid; w < W; w += TK_NT) { s.xb[w] = 0; s.yb[w] = 0; }
-    __syncthreads();
-    // pieces are read TK_LD at a time per thread, so their loads overlap
+    // Pieces of a tile with at most ~2000 pieces are staged in the (still unused) phase C/D region by
+    // bulk copies, their ranks kept next to them; each operand starts at the source's offset modulo 16
+    // bytes so both ends of the copy are 16-byte aligned, a leading / trailing odd piece is loaded plainly.
+    constexpr int DB = (int)(sizeof(s.lb) + sizeof(s.lp) + sizeof(s.lv) + sizeof(s.ca) + sizeof(s.cb) +
+                             sizeof(s.mc) + sizeof(s.srow));
     const unsigned long long* pa = s.pa;
     const unsigned long long* pb = s.pb;
+    // A pieces at sp + offA, B pieces at sp + offB: offsets of the parity of the source addresses' 8-byte
+    // index, so a piece and its copy agree modulo 16 bytes
+    const int offA = nA ? (int)(((uintptr_t)pa >> 3) & 1) : 0;
+    const int pbit = nB ? (int)(((uintptr_t)pb >> 3) & 1) : 0;
+    const int offB = offA + nA + (((offA + nA) & 1) != pbit ? 1 : 0);
+    const int rkoff = ((offB + nB) * 8 + 15) & ~15;  // bytes
+    const bool pst = rkoff + P * 16 <= DB;
+    unsigned long long* sp = reinterpret_cast<unsigned long long*>(s.dbuf);
+    int4* srk = reinterpret_cast<int4*>(s.dbuf + rkoff);
+    if (pst) {
+      // bulk parts [a0, a1) of A and [b0, b1) of B: even counts of pieces starting on 16-byte addresses
+      const int a0 = offA & 1, a1 = nA > a0 ? a0 + ((nA - a0) & ~1) : a0;
+      const int b0 = pbit, b1 = nB > b0 ? b0 + ((nB - b0) & ~1) : b0;
+      if (tid == 0) {
+        const unsigned bytes = (unsigned)(a1 - a0 + b1 - b0) * 8u;
+        asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(mbar),
+                     "r"(bytes)
+                     : "memory");
+        if (a1 > a0) tk_bulk(sp + offA + a0, pa + a0, (unsigned)(a1 - a0) * 8u, mbar);
+        if (b1 > b0) tk_bulk(sp + offB + b0, pb + b0, (unsigned)(b1 - b0) * 8u, mbar);
+      }
+      // the first / last piece of an operand when it lies outside the bulk part
+      if (tid < 4) {
+        const int i = (tid & 1) ? ((tid < 2 ? nA : nB) - 1) : 0;
+        if (tid < 2 && nA && (i < a0 || i >= a1)) sp[offA + i] = pa[i];
+        if (tid >= 2 && nB && (i < b0 || i >= b1)) sp[offB + i] = pb[i];
+      }
+    }
+    for (int w = tid; w < W; w += TK_NT) { s.xb[w] = 0; s.yb[w] = 0; }
+    if (pst) {
+      const bool ok = tk_wait(mbar, mph, TK_SPIN_LIMIT);
+      mph ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) gb_set_error(st, GB_ERR_TIMEOUT, KID_TILE_COPY, t);
+        tk_wait(mbar, mph ^ 1u, TK_SPIN_LIMIT);  // let copies in flight land before the CTA exits
+        return;
+      }
+      pa = sp + offA;
+      pb = sp + offB;
+    } else {
+      __syncthreads();
+    }
+    // pieces are read TK_LD at a time per thread, so their loads overlap
     for (int i0 = tid; i0 < P; i0 += TK_LD * TK_NT) {
       unsigned long long pk[TK_LD];
 #pragma unroll
@@ -615,7 +661,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       if (tid == 0) {
         s.Xt = (int*)sc_up(s, base, half, (unsigned long long)Nx * 4);
         s.Yt = (int*)sc_up(s, base, half, (unsigned long long)Ny * 4);
-        s.rk = (int4*)sc_up(s, base, half, (unsigned long long)P * 16);
+        s.rk = pst ? srk : (int4*)sc_up(s, base, half, (unsigned long long)P * 16);
       }
       __syncthreads();
       if (!s.err) {
