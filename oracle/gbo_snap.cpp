@@ -258,7 +258,7 @@ int64_t orc_snappy_max_length(int64_t len) { return 32 + len + len / 6; }
 // 65536-byte fragments compressed independently (offsets never reach before
 // the fragment).  Every position p with 4 bytes left in the fragment has a
 // candidate: the latest earlier position whose 4 bytes hash to the same slot
-// ((v * 0x9E3779B1) >> 20, Knuth's multiplicative hash into 4096 slots;
+// ((v * 0x9E3779B1) >> 21, Knuth's multiplicative hash into 2048 slots;
 // every position is hashed, including those inside matches).  The parse
 // starts at 0; at p, when the candidate's 4 bytes equal those at p, the match
 // is extended as far as the fragment allows and, when at least 8 bytes long,
@@ -269,13 +269,13 @@ int64_t orc_snappy_max_length(int64_t len) { return 32 + len + len / 6; }
 // when 4..11 long with offset < 2048, else a 2-byte-offset copy.
 int64_t orc_snappy_compress(const uint8_t* in, int64_t len, uint8_t* out) {
   int64_t o = put_varint(out, (uint64_t)len);
-  std::vector<uint32_t> table(4096), cand(65536);
+  std::vector<uint32_t> table(2048), cand(65536);
   for (int64_t f0 = 0; f0 < len; f0 += 65536) {
     const int64_t fl = len - f0 < 65536 ? len - f0 : 65536;
     const uint8_t* s = in + f0;
     std::fill(table.begin(), table.end(), 0u);
     for (int64_t p = 0; p + 4 <= fl; ++p) {  // candidate of every position (1-based, 0 = none)
-      const uint32_t h = (ld32(s + p) * 0x9E3779B1u) >> 20;
+      const uint32_t h = (ld32(s + p) * 0x9E3779B1u) >> 21;
       cand[p] = table[h];
       table[h] = (uint32_t)p + 1u;
     }

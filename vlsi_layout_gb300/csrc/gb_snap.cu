@@ -20,8 +20,8 @@
 //     second writes them.
 // Snappy: each 65536-byte fragment of a chunk's codec bytes is compressed by
 // one warp, 32 positions at a time: a position's candidate is the latest
-// earlier position with the same 12-bit hash of its 4 bytes (warp match for
-// the batch, a 4096-slot table across batches); the greedy parse jumps to
+// earlier position with the same 11-bit hash of its 4 bytes (warp match for
+// the batch, a 2048-slot table across batches); the greedy parse jumps to
 // the next verified candidate, extends the match 32 bytes per step and, when
 // it is at least 8 bytes long, emits Snappy literal / copy elements.  Fragments are concatenated behind the
 // chunk's length preamble.  Decoding takes one warp per chunk through the
@@ -684,12 +684,12 @@ __global__ void __launch_bounds__(256)
 k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __restrict__ fsrc,
                   const int* __restrict__ flen, long long nfrag, unsigned char* __restrict__ fout,
                   int* __restrict__ flout, DStatus* st) {
-  extern __shared__ unsigned short table[];  // [8][4096]: latest position + 1 (positions with 4 bytes left are < 65533)
+  extern __shared__ unsigned short table[];  // [8][2048]: latest position + 1 (positions with 4 bytes left are < 65533)
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long f = (long long)blockIdx.x * 8 + wid;
   if (f >= nfrag) return;
-  unsigned short* tab = table + wid * 4096;
-  for (int i = lane; i < 4096; i += 32) tab[i] = 0;
+  unsigned short* tab = table + wid * 2048;
+  for (int i = lane; i < 2048; i += 32) tab[i] = 0;
   __syncwarp();
   const unsigned char* src = raw + fsrc[f];
   const int fl = flen[f];
@@ -699,7 +699,7 @@ k_snappy_compress(const unsigned char* __restrict__ raw, const long long* __rest
     const int q = bb + lane;
     const bool has = q + 4 <= fl;
     const unsigned v = has ? sn_ld32(src + q) : 0u;
-    const unsigned h = (v * 0x9E3779B1u) >> 20;
+    const unsigned h = (v * 0x9E3779B1u) >> 21;
     const unsigned peers = __match_any_sync(0xffffffffu, has ? h : 0x10000u + lane);
     const unsigned lower = peers & ((1u << lane) - 1u);
     unsigned cand = 0;  // 1-based
@@ -1043,8 +1043,8 @@ int snap_encode(gb_context* ctx, const int4* d_boxes, long long n, int method, u
   if (nfrag) {
     cudaMemcpyAsync(d_fsrc, fsrc.data(), nfrag * 8, cudaMemcpyHostToDevice, c.stream);
     cudaMemcpyAsync(d_flen, flen.data(), nfrag * 4, cudaMemcpyHostToDevice, c.stream);
-    cudaFuncSetAttribute((const void*)k_snappy_compress, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 4096 * 2);
-    k_snappy_compress<<<(unsigned)((nfrag + 7) / 8), 256, 8 * 4096 * 2, c.stream>>>(d_raw, d_fsrc, d_flen, nfrag, d_fout,
+    cudaFuncSetAttribute((const void*)k_snappy_compress, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * 2048 * 2);
+    k_snappy_compress<<<(unsigned)((nfrag + 7) / 8), 256, 8 * 2048 * 2, c.stream>>>(d_raw, d_fsrc, d_flen, nfrag, d_fout,
                                                                                     d_flout, c.st);
     ++c.launches;
   }
