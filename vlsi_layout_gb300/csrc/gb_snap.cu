@@ -419,34 +419,26 @@ __device__ __forceinline__ int sn_vl(const unsigned* cont, int q) {  // varint l
   return k <= 10 ? k : 0;
 }
 
+// Branch-free: every field's varint length is looked up and selected by the
+// infobyte's bits, so the lanes of a warp (at different bytes) do not diverge.
 __device__ __forceinline__ int sn_rec_len_bits(const unsigned char* buf, const unsigned* cont, int b) {
   const unsigned info = buf[b];
-  int l = 1, k;
-  if (info & 32) {
-    if (!(k = sn_vl(cont, b + l))) return 0;
-    l += k;
-  }
-  if (info & 64) {
-    if (!(k = sn_vl(cont, b + l))) return 0;
-    l += k;
-  }
-  if (info & 1) {
-    if (info & 2) {
-      if (!(k = sn_vl(cont, b + l))) return 0;
-      l += k;
-    } else {
-      l += 2;
-    }
-  }
-  if ((info & 20) == 4) {
-    if (info & 8) {
-      if (!(k = sn_vl(cont, b + l))) return 0;
-      l += k;
-    } else {
-      l += 2;
-    }
-  }
-  return l;
+  int l = 1;
+  bool bad = false;
+  int k = sn_vl(cont, b + l);
+  bad |= (info & 32) && !k;
+  l += (info & 32) ? k : 0;
+  k = sn_vl(cont, b + l);
+  bad |= (info & 64) && !k;
+  l += (info & 64) ? k : 0;
+  k = sn_vl(cont, b + l);
+  bad |= (info & 3) == 3 && !k;
+  l += (info & 1) ? ((info & 2) ? k : 2) : 0;
+  k = sn_vl(cont, b + l);
+  const bool hf = (info & 20) == 4;
+  bad |= hf && (info & 8) && !k;
+  l += hf ? ((info & 8) ? k : 2) : 0;
+  return bad ? 0 : l;
 }
 
 __global__ void __launch_bounds__(SN_BT)
