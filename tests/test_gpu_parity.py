@@ -244,3 +244,15 @@ def test_op1_area_cells(ctx, oracle, amount):
         ea = np.array([oracle.union_area(boxes[off[k]:off[k + 1]]) for k in range(len(off) - 1)])
     assert np.array_equal(area, ea)
     assert area[3] == 0 and area[17] == 0
+
+
+def test_op1_host_two_groups(ctx, oracle):
+    """gb_op1_host on a layout large enough to be split into two groups of cells
+    (the second group's upload overlaps the first group's deck): per-cell counts
+    and areas equal the oracle's."""
+    boxes, off = cells_layout(400, median=8000, seed=41)
+    assert off[-1] >= (1 << 22)
+    b = np.ascontiguousarray(boxes, np.int32)
+    counts, area, fails = ctx.op1_host(b.ctypes.data, len(b), off, 1)
+    ec, ea = oracle.op1_cells(b, off)
+    assert np.array_equal(counts, ec) and np.array_equal(area, ea) and fails == 0

@@ -323,6 +323,8 @@ extern "C" int gb_context_destroy(gb_context* ctx) {
   cudaFree(c.tile_counter);
   cudaFree(c.desc);
   cudaFree(c.tile_scratch);
+  if (c.io_buf) cudaFree(c.io_buf);
+  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   gb_radix_free(c);
   if (c.own_stream) cudaStreamDestroy(c.stream);
   if (ctx == g_default) g_default = nullptr;
@@ -419,8 +421,9 @@ extern "C" int gb_set_tile_scratch(gb_context* ctx, unsigned long long bytes) {
 }
 
 // ======================================================================= layers
+// borrow: boxes is a device pointer used in place (coff then a host pointer).
 static int make_raw_layer(gb_context* ctx, const c_box* boxes, unsigned long long n,
-                          const long long* coff, int ncell, bool device_src, gb_layer** out) {
+                          const long long* coff, int ncell, bool device_src, gb_layer** out, bool borrow = false) {
   if (!ctx || !out || ncell < 1) return GB_ERR_ARG;
   *out = nullptr;
   GbCtx& c = ctx->c;
@@ -432,23 +435,23 @@ static int make_raw_layer(gb_context* ctx, const c_box* boxes, unsigned long lon
   L->ncell = ncell;
   L->binned = 0;
   L->nbox_host = (long long)n;
-  void *pb = nullptr, *pc = nullptr, *pcell = nullptr;
-  if (cudaMalloc(&pb, std::max<size_t>(16, n * 16)) != cudaSuccess ||
+  void *pb = borrow ? (void*)boxes : nullptr, *pc = nullptr, *pcell = nullptr;
+  if ((!borrow && cudaMalloc(&pb, std::max<size_t>(16, n * 16)) != cudaSuccess) ||
       cudaMalloc(&pc, (size_t)(ncell + 1) * 8) != cudaSuccess ||
       cudaMalloc(&pcell, (size_t)ncell * (16 + 8 + 8 + 16) + (size_t)(ncell + 1) * 8) != cudaSuccess) {
-    if (pb) cudaFree(pb);
+    if (pb && !borrow) cudaFree(pb);
     if (pc) cudaFree(pc);
     c.desc_free.push_back(s);
     delete L;
     return set_err(ctx, GB_ERR_OOM, "cudaMalloc failed for a layer");
   }
-  L->own_boxes = pb;
+  L->own_boxes = borrow ? nullptr : pb;
   L->own_coff = pc;
   L->own_cell = pcell;
   const cudaMemcpyKind kind = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if (n) cudaMemcpyAsync(pb, boxes, n * 16, kind, c.stream);
+  if (n && !borrow) cudaMemcpyAsync(pb, boxes, n * 16, kind, c.stream);
   if (coff) {
-    cudaMemcpyAsync(pc, coff, (size_t)(ncell + 1) * 8, kind, c.stream);
+    cudaMemcpyAsync(pc, coff, (size_t)(ncell + 1) * 8, borrow ? cudaMemcpyHostToDevice : kind, c.stream);
   } else {
     long long h[2] = {0, (long long)n};
     cudaMemcpyAsync(pc, h, 16, cudaMemcpyHostToDevice, c.stream);
@@ -473,6 +476,13 @@ static int make_raw_layer(gb_context* ctx, const c_box* boxes, unsigned long lon
   *out = L;
   return GB_OK;
 }
+
+namespace gbi {
+int layer_over_device(gb_context* ctx, const void* d_boxes, long long n, const long long* h_offsets, int ncell,
+                      gb_layer** out) {
+  return make_raw_layer(ctx, (const c_box*)d_boxes, (unsigned long long)n, h_offsets, ncell, true, out, true);
+}
+}  // namespace gbi
 
 extern "C" int gb_layer_from_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
                                   const long long* cell_offsets, int ncell, gb_layer** out) {

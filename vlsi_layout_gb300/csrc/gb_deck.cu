@@ -16,6 +16,8 @@
 #include <vector>
 
 #include "gbool.h"
+#include <algorithm>
+
 #include "gb_internal.h"
 
 #define GB_GRID_TUNE_MIN 13  // smallest tile grid (log2 dbu) the slab-height tuner tries
@@ -221,31 +223,90 @@ __global__ void k_gather_counts(const DLayer* const* L, int nl, int ncell, long 
   }
 }
 
+// The deck through host buffers.  The boxes go to a device staging buffer
+// kept by the context (grown when needed) on a copy stream, in two halves
+// split at a cell boundary when the layer is large; each half's deck starts
+// when its copy has landed, so the second copy overlaps the first half's
+// work.  Counts and areas come back with one copy each at the end.
 extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
                            const long long* cell_offsets, int ncell, int32_t a, long long* counts,
                            long long* area, int* assert_failures) {
   if (!ctx || (!boxes && n) || ncell < 1) return GB_ERR_ARG;
   if (!cell_offsets) ncell = 1;
   GbCtx& c = ctx->c;
-  gb_layer* P = nullptr;
-  int e = gb_layer_from_host(ctx, boxes, n, cell_offsets, ncell, &P);
-  if (e) return e;
+  std::vector<long long> off(ncell + 1);
+  if (cell_offsets) {
+    std::copy(cell_offsets, cell_offsets + ncell + 1, off.begin());
+    for (int k = 0; k < ncell; ++k)
+      if (off[k] > off[k + 1] || off[k] < 0) return set_err(ctx, GB_ERR_ARG, "cell offsets must not decrease");
+    if (off[ncell] > (long long)n) return set_err(ctx, GB_ERR_ARG, "cell offsets past the boxes");
+  } else {
+    off[0] = 0;
+    off[1] = (long long)n;
+  }
+  const size_t bytes = std::max<size_t>(16, (size_t)n * 16);
+  if (c.io_cap < bytes) {
+    if (c.io_buf) cudaFree(c.io_buf);
+    c.io_buf = nullptr;
+    c.io_cap = 0;
+    if (cudaMalloc(&c.io_buf, bytes) != cudaSuccess) return set_err(ctx, GB_ERR_OOM, "input staging buffer");
+    c.io_cap = bytes;
+  }
+  if (!c.copy_stream && cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return set_err(ctx, GB_ERR_CUDA, "copy stream");
+  // groups of cells: two halves of the boxes when there are enough of them
+  std::vector<int> cut{0};
+  if (ncell > 1 && n >= (1ull << 22)) {
+    const int k = (int)(std::lower_bound(off.begin(), off.end(), (long long)(n / 2)) - off.begin());
+    if (k > 0 && k < ncell) cut.push_back(k);
+  }
+  cut.push_back(ncell);
+  const int ng = (int)cut.size() - 1;
+  std::vector<cudaEvent_t> ev(ng);
+  char* dbox = (char*)c.io_buf;
+  // the copy stream starts after the work already queued on the context stream (earlier users of the buffer)
+  cudaEvent_t ready;
+  cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  cudaEventRecord(ready, c.stream);
+  cudaStreamWaitEvent(c.copy_stream, ready, 0);
+  for (int g = 0; g < ng; ++g) {
+    cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming);
+    const long long b0 = off[cut[g]], b1 = off[cut[g + 1]];
+    if (b1 > b0)
+      cudaMemcpyAsync(dbox + b0 * 16, boxes + b0, (size_t)(b1 - b0) * 16, cudaMemcpyHostToDevice, c.copy_stream);
+    cudaEventRecord(ev[g], c.copy_stream);
+  }
   long long* dcounts = nullptr;
   long long* darea = nullptr;
   DLayer** dl = nullptr;
-  cudaMalloc(&dcounts, (size_t)ncell * 6 * 8);
-  cudaMalloc(&darea, (size_t)ncell * 8);
-  cudaMalloc(&dl, 8 * sizeof(DLayer*));
-  e = gb_run_retry(ctx, [&]() -> int {
-    gb_layer* outs[6];
-    int r = gb_op1_area(ctx, P, a, outs, darea);
-    if (r) return r;
-    DLayer* hl[6];
-    for (int j = 0; j < 6; ++j) hl[j] = outs[j]->d;
-    cudaMemcpyAsync(dl, hl, sizeof(hl), cudaMemcpyHostToDevice, c.stream);
-    k_gather_counts<<<(ncell + 255) / 256, 256, 0, c.stream>>>(dl, 6, ncell, dcounts, nullptr, nullptr, c.st);
-    return GB_OK;
-  });
+  int e = GB_OK;
+  if (cudaMalloc(&dcounts, (size_t)ncell * 6 * 8) != cudaSuccess || cudaMalloc(&darea, (size_t)ncell * 8) != cudaSuccess ||
+      cudaMalloc(&dl, 8 * sizeof(DLayer*)) != cudaSuccess)
+    e = set_err(ctx, GB_ERR_OOM, "deck result buffers");
+  for (int g = 0; g < ng && !e; ++g) {
+    const int k0 = cut[g], k1 = cut[g + 1];
+    const long long b0 = off[k0];
+    std::vector<long long> goff(off.begin() + k0, off.begin() + k1 + 1);
+    for (long long& v : goff) v -= b0;
+    cudaStreamWaitEvent(c.stream, ev[g], 0);
+    gb_layer* P = nullptr;
+    e = gbi::layer_over_device(ctx, dbox + b0 * 16, off[k1] - b0, goff.data(), k1 - k0, &P);
+    if (e) break;
+    const int gn = k1 - k0;
+    e = gb_run_retry(ctx, [&]() -> int {
+      gb_layer* outs[6];
+      int r = gb_op1_area(ctx, P, a, outs, darea + k0);
+      if (r) return r;
+      DLayer* hl[6];
+      for (int j = 0; j < 6; ++j) hl[j] = outs[j]->d;
+      cudaMemcpyAsync(dl, hl, sizeof(hl), cudaMemcpyHostToDevice, c.stream);
+      k_gather_counts<<<(gn + 255) / 256, 256, 0, c.stream>>>(dl, 6, gn, dcounts + (size_t)k0 * 6, nullptr, nullptr,
+                                                             c.st);
+      return GB_OK;
+    });
+    gb_layer_free(ctx, P);
+  }
+  cudaStreamSynchronize(c.copy_stream);  // no copy may outlive the call
   std::vector<long long> hc((size_t)ncell * 6), ha(ncell);
   if (!e) {
     cudaMemcpy(hc.data(), dcounts, hc.size() * 8, cudaMemcpyDeviceToHost);
@@ -256,10 +317,11 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
     if (counts) memcpy(counts, hc.data(), hc.size() * 8);
     if (area) memcpy(area, ha.data(), ha.size() * 8);
   }
-  cudaFree(dcounts);
-  cudaFree(darea);
-  cudaFree(dl);
-  gb_layer_free(ctx, P);
+  for (cudaEvent_t x : ev) cudaEventDestroy(x);
+  cudaEventDestroy(ready);
+  if (dcounts) cudaFree(dcounts);
+  if (darea) cudaFree(darea);
+  if (dl) cudaFree(dl);
   return e;
 }
 

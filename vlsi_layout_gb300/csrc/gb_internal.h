@@ -43,6 +43,9 @@ struct GbCtx {
   long long launches = 0;            // kernels issued by the engine (host-side count)
   void* rs = nullptr;                // radix sort state (histograms, look-back status), gb_radix.cu
   int grid = 16;                     // tile grid log2 (slab height 2^grid dbu) of the operators
+  void* io_buf = nullptr;            // device staging of host inputs (gb_op1_host), grow-only
+  size_t io_cap = 0;
+  cudaStream_t copy_stream = nullptr;  // host-to-device copies that overlap the compute stream
 };
 
 struct gb_layer {
@@ -79,6 +82,10 @@ gb_layer* new_arena_layer(gb_context* ctx, int ncell, int g);
 gb_layer* binned_of(gb_context* ctx, gb_layer* L, int g);
 DStatus read_status(gb_context* ctx);
 DLayer read_desc(gb_context* ctx, gb_layer* L);
+// A raw layer over n boxes already in device memory (not copied; the caller
+// keeps them alive while the layer is used), cells given by host offsets.
+int layer_over_device(gb_context* ctx, const void* d_boxes, long long n, const long long* h_offsets, int ncell,
+                      gb_layer** out);
 }
 gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode);
 gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge);
