@@ -299,7 +299,7 @@ int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, long l
  * union area of P (area[ncell], may be NULL) are copied out.  Layers of 4M
  * boxes or more run as two groups of cells whose uploads overlap the first
  * group's work (pinned host memory makes the copies asynchronous); the
- * device staging buffer stays with the context until it is destroyed. */
+ * device staging buffer stays with the context until it is destroyed.
  * *assert_failures receives the number of failing ASSERT_ZEROs. */
 int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
                 const long long* cell_offsets, int ncell, int32_t a, long long* counts,
