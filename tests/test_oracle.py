@@ -85,9 +85,23 @@ def test_complement_identity(oracle):
 def test_oracle_matches_bruteforce(oracle, op, seed):
     A = random_layer(40, die=3000, wmin=5, wmax=600, seed=seed, x0=-1500)
     B = random_layer(40, die=3000, wmin=5, wmax=600, seed=seed + 50, y0=-800)
-    for g in (16, 10):
+    for g in (16, 13, 10):
         r = oracle.boolean(A, B, op, g)
         assert r.tolist() == brute(A, B, op, g).tolist()
+
+
+@pytest.mark.parametrize("g", [16, 14, 13])
+def test_grow_and_dilation_match_bruteforce(oracle, g):
+    """GROW (box_grow_directional, then heal) and SIZE +s (Minkowski dilation of
+    the union = union of the dilated boxes) on the tile grids the slab-height
+    tuner chooses from: the union of the moved boxes, rasterised independently."""
+    A = random_layer(60, die=40000, wmin=5, wmax=3000, seed=g, x0=-20000, y0=-9000)
+    for E, N, W, S in ((3, 1, 2, 5), (700, 0, 0, 1300)):
+        G = A.astype(np.int64) + np.array([-W, -S, E, N])
+        assert oracle.grow(A, E, N, W, S, g).tolist() == brute(G, G[:0], 4, g).tolist()
+    for s_ in (1, 2500):
+        D = A.astype(np.int64) + np.array([-s_, -s_, s_, s_])
+        assert oracle.size(A, s_, g).tolist() == brute(D, D[:0], 4, g).tolist()
 
 
 def test_point_set_identities(oracle):
