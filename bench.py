@@ -487,6 +487,50 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
     return res
 
 
+def events_leg(n=50_000_000, steps=2):
+    """Tracker event sort (sort_event_trackers -> device_event_sort,
+    event_sorter.cu:48-81: trackers ordered by (X, Y) through 64-bit packed
+    keys) of n trackers with coordinates uniform in a 4e7 die: the drop-in on
+    a host array (H2D and D2H inside, as the Fortran layer calls it) and on a
+    device array; the output keys are checked against numpy's sort of the
+    input keys."""
+    import torch
+    from vlsi_layout_gb300 import engine
+    rng = np.random.default_rng(6)
+    t = np.zeros(n, engine.TRACKER_DTYPE)
+    t["X"] = rng.integers(-20_000_000, 20_000_000, n)
+    t["Y"] = rng.integers(-20_000_000, 20_000_000, n)
+    t["polygonNumber"] = rng.choice(np.array([-1, 1], np.int8), n)
+    L = engine.lib()
+    th, td = [], []
+    out = None
+    for it in range(steps + 1):
+        h = t.copy()
+        t0 = time.perf_counter()
+        L.device_event_sort(h.ctypes.data, n)
+        t1 = time.perf_counter()
+        d = torch.from_numpy(t.view(np.uint8)).cuda()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        L.device_event_sort(d.data_ptr(), n)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        if it:
+            th.append(t1 - t0)
+            td.append(t3 - t2)
+        out = h
+        del d
+    def keys(a):
+        return ((a["X"].astype(np.int64) + 2**31).astype(np.uint64) << np.uint64(32)) | \
+            (a["Y"].astype(np.int64) + 2**31).astype(np.uint64)
+    ok = bool(np.array_equal(keys(out), np.sort(keys(t))))
+    sh, sd = statistics.median(th), statistics.median(td)
+    return {"n": n, "host_s": sh, "host_trackers_per_s": n / sh, "device_s": sd, "device_trackers_per_s": n / sd,
+            "sorted_keys_equal_numpy": ok,
+            "timing": "host wall clock around device_event_sort (host array: H2D + D2H inside; device array)",
+            "reference": "GPU radix sort of 314,159,232 x 4 trackers in 5.96 s on a DGX Spark (NOTES.txt:595-596)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -511,6 +555,8 @@ def main():
     ap.add_argument("--grid", default="auto", help="tile grid log2 (slab height) of the deck, or 'auto' to tune")
     ap.add_argument("--snap-only", action="store_true")
     ap.add_argument("--conn-only", action="store_true")
+    ap.add_argument("--events-only", action="store_true")
+    ap.add_argument("--no-events", action="store_true")
     ap.add_argument("--no-conn", action="store_true")
     ap.add_argument("--no-snap", action="store_true")
     ap.add_argument("--snap-n", type=int, default=10_000_000, help="boxes per stdcell layer of the SNAP leg")
@@ -520,6 +566,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         print(json.dumps({"sort": sort_leg(n=args.sort_n, steps=args.steps, tune=not args.sort_no_tune)}), flush=True)
+        return
+    if args.events_only:
+        import torch
+        torch.cuda.set_device(local)
+        print(json.dumps({"event_sort": events_leg(steps=args.steps)}), flush=True)
         return
     if args.conn_only:
         import torch
@@ -678,6 +729,9 @@ def main():
     conn = None
     if rank == 0 and not args.no_conn:
         conn = connectivity_leg(steps=2)
+    events = None
+    if rank == 0 and not args.no_events:
+        events = events_leg(steps=2)
     value = replica_value(world, nbox, ms)
     out = {
         "metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
@@ -708,6 +762,7 @@ def main():
         "sort": sort,
         "snap": snap,
         "connectivity": conn,
+        "event_sort": events,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
