@@ -231,17 +231,19 @@ int32_t gb_um_to_dbu(double r);
  * serving loop that reserved its whole device budget up front, a host that
  * must avoid the allocator's implicit device synchronisation, or a Fortran /
  * C caller that owns only the buffers it passes.  Computes the canonical
- * strips of pred(A, B) (op 0..4) for device boxes d_A[nA], d_B[nB] that all
- * lie in one 65536-dbu tile, into d_out[out_cap]; *d_count (device) gets the
- * strip count or -1, *d_area (device, may be NULL) the strip area.  Works
- * only in storage reserved statically in the library (each GPU that loads it
- * holds ~9 MB until exit): nA + nB <= 16384 and at most 65536 strips, else
- * GB_ERR_CAPACITY.  Boxes outside the first box's tile give
- * GB_ERR_INVALID_BOX.  The first call on a device sets up the static storage
+ * strips of pred(A, B) (op 0..4; MERGE reads A only) for device boxes
+ * d_A[nA], d_B[nB] that all lie in one 65536-dbu tile, into d_out[out_cap];
+ * *d_count (device) gets the strip count, *d_area (device, may be NULL) the
+ * strip area.  Works only in storage reserved statically in the library
+ * (each GPU that loads it holds ~9 MB until exit): nA + nB <= 16384 and at
+ * most 65536 strips, else GB_ERR_CAPACITY; a result larger than out_cap is
+ * GB_ERR_CAPACITY too.  Boxes outside the first box's tile give
+ * GB_ERR_INVALID_BOX.  On every status other than GB_OK, *d_count (and
+ * *d_area) is -1.  The first call on a device sets up the static storage
  * (cudaGetSymbolAddress) and should come before any stream capture.  All
- * calls share that storage: calls whose GPU work overlaps race.  The call
- * synchronises `stream` (a cudaStream_t, NULL = default) and returns the
- * status. */
+ * calls share that storage: calls whose GPU work overlaps race.  Every call
+ * waits for `stream` (a cudaStream_t, NULL = default) to finish and returns
+ * the status. */
 int gb_bool_tile_noalloc(int op, const c_box* d_A, int nA, const c_box* d_B, int nB, c_box* d_out,
                          long long out_cap, long long* d_count, long long* d_area, void* stream);
 

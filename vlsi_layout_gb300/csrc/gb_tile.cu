@@ -1,6 +1,7 @@
 // gb_tile.cu -- the scanline Boolean kernel.
 //
-// One persistent CTA per SM pulls output tiles from a device work counter.
+// Persistent CTAs (three per SM, 8 warps each) pull output tiles from a
+// device work counter.
 // For a tile it computes the canonical strips of pred(A, B) inside the tile:
 // at every x the maximal y-intervals of the region, merged along x while
 // unchanged -- the decomposition heal_boxes emits (polygon_fracture.f90:
@@ -31,7 +32,9 @@
 //     sub-band with the same y-interval; every chain head becomes one strip.
 //     Strips are written in (sub-band, column, row) order, so the output of a
 //     tile is deterministic.
-// No piece ever waits on another CTA: there is no spin-wait in this kernel.
+// No CTA ever waits on another CTA.  The only waits are on the CTA's own
+// mbarrier for the bulk copies of phases A and D; each is bounded (a poll
+// limit, then GB_ERR_TIMEOUT and the CTA leaves after its copies land).
 #include <cstdio>
 #include <mutex>
 
@@ -1007,14 +1010,17 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
 // this library: every GPU that loads libgbool.so holds this storage until the
 // process exits.
 //
-// Limits: nA + nB <= GB_NA_MAX_IN boxes, at most GB_NA_MAX_OUT result strips,
-// and the CTA scratch of GB_NA_SCRATCH bytes.  Beyond any of them the call
-// returns GB_ERR_CAPACITY and leaves *d_count at -1.
+// Limits: nA + nB <= GB_NA_MAX_IN boxes (nA alone for MERGE, which ignores
+// B), at most GB_NA_MAX_OUT result strips, and the CTA scratch of
+// GB_NA_SCRATCH bytes.  Beyond any of them the call returns GB_ERR_CAPACITY;
+// a result with more strips than the caller's out_cap does too.  On every
+// status other than GB_OK, *d_count (and *d_area when given) is -1.
 //
 // All calls share the static storage (each call re-initialises what must
 // start at zero and keeps the last call's contents otherwise), so calls whose
 // work overlaps on the GPU -- on different streams, or from different host
-// threads -- race and must be serialised by the caller.
+// threads -- race and must be serialised by the caller.  Every call waits for
+// its stream to finish before it returns.
 //
 // Set-up: the first call on a device resolves the device addresses of the
 // static storage with cudaGetSymbolAddress (with that device current) and
@@ -1025,9 +1031,16 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
 #define GB_NA_SCRATCH (8u << 20)
 #define GB_NA_MAX_DEV 64
 
+// What the host reads back after a call, in one copy: the status and the
+// result's strip count (also when it exceeds the caller's buffer).
+struct NoAllocResult {
+  DStatus st;       // status; its arena is empty (no spill space)
+  long long nout;   // strips of the result
+};
+
 struct NoAllocState {
+  NoAllocResult res;
   DLayer L[3];                              // A, B, result
-  DStatus st;                               // status; its arena is empty (no spill space)
   long long ctr[64];                        // work counters of the tile kernel
   int4 win[3];
   long long tbase[3][2];
@@ -1049,15 +1062,17 @@ static std::mutex g_na_mu;
 
 // Re-initialise the shared state and pack the inputs (one block).  Every box
 // must lie inside the tile of the first box; otherwise the status says so.
+// MERGE reads A only.
 __global__ void k_na_prep(NoAllocState* S, int op, const int4* A, int nA, const int4* B, int nB, int g) {
   __shared__ int bad;
   __shared__ int tx0, ty0;
+  if (op == GB_OP_MERGE) nB = 0;
   if (threadIdx.x == 0) {
     bad = 0;
     const int4 f = nA ? A[0] : (nB ? B[0] : make_int4(0, 0, 1, 1));
     tx0 = gb_floor_shift(f.x, g);
     ty0 = gb_floor_shift(f.y, g);
-    memset(&S->st, 0, sizeof(S->st));  // empty arena: spills report GB_ERR_CAPACITY
+    memset(&S->res, 0, sizeof(S->res));  // empty arena: spills report GB_ERR_CAPACITY
     for (int i = 0; i < 64; ++i) S->ctr[i] = 0;
   }
   __syncthreads();
@@ -1073,7 +1088,7 @@ __global__ void k_na_prep(NoAllocState* S, int op, const int4* A, int nA, const 
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (bad) gb_set_error(&S->st, GB_ERR_INVALID_BOX, 60, 0);
+    if (bad) gb_set_error(&S->res.st, GB_ERR_INVALID_BOX, 60, 0);
     for (int l = 0; l < 3; ++l) {
       DLayer& d = S->L[l];
       memset(&d, 0, sizeof(d));
@@ -1101,7 +1116,7 @@ __global__ void k_na_prep(NoAllocState* S, int op, const int4* A, int nA, const 
     S->L[0].npcs = S->L[0].nused = S->L[0].ntot = nA;
     S->L[1].pcs = S->pcs_in;
     S->tstart[1][0] = nA;
-    S->tcount[1][0] = op == GB_OP_MERGE ? 0 : nB;
+    S->tcount[1][0] = nB;
     S->L[1].npcs = S->L[1].nused = S->L[1].ntot = nB;
     S->L[2].pcs = S->pcs_out;
     S->L[2].npcs = GB_NA_MAX_OUT;
@@ -1112,16 +1127,20 @@ __global__ void k_na_prep(NoAllocState* S, int op, const int4* A, int nA, const 
 }
 
 // Unpack the result into the caller's buffer; *count = strips, or -1 when the
-// call failed or the buffer is too small.
-__global__ void k_na_export(const NoAllocState* S, int4* out, long long cap, long long* count, long long* area) {
+// call failed or the buffer is too small.  The strip count also goes to the
+// state, for the host.
+__global__ void k_na_export(NoAllocState* S, int4* out, long long cap, long long* count, long long* area) {
   const DLayer& O = S->L[2];
   const long long n = O.ntiles ? O.tcount[0] : 0;
-  const bool ok = S->st.err == 0 && n <= cap;
+  const bool ok = S->res.st.err == 0 && n <= cap;
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     *count = ok ? n : -1;
     if (area) *area = ok ? S->cell_area[2] : -1;
   }
-  if (!ok) return;
+  if (!ok) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) S->res.nout = n;
+    return;
+  }
   const int4 w = S->win[2];
   const int ox = w.x << O.g, oy = w.y << O.g;
   const unsigned long long* p = O.pcs + O.tstart[0];
@@ -1130,18 +1149,32 @@ __global__ void k_na_export(const NoAllocState* S, int4* out, long long cap, lon
     gb_unpack(p[i], a, b, c, d);
     out[i] = make_int4(ox + a, oy + b, ox + c, oy + d);
   }
+  if (threadIdx.x == 0 && blockIdx.x == 0) S->res.nout = n;
+}
+
+// *d_count = -1 (and *d_area) for a call refused before its kernels run.
+static int na_refuse(int code, long long* d_count, long long* d_area, cudaStream_t s) {
+  if (d_count) cudaMemsetAsync(d_count, 0xff, sizeof(long long), s);
+  if (d_area) cudaMemsetAsync(d_area, 0xff, sizeof(long long), s);
+  if (d_count || d_area) cudaStreamSynchronize(s);
+  return code;
 }
 
 extern "C" int gb_bool_tile_noalloc(int op, const int4* d_A, int nA, const int4* d_B, int nB, int4* d_out,
                                     long long out_cap, long long* d_count, long long* d_area, void* stream) {
-  if (op < GB_OP_XOR || op > GB_OP_MERGE || nA < 0 || nB < 0 || !d_out || !d_count) return GB_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (op == GB_OP_MERGE) nB = nB < 0 ? nB : 0;
+  if (op < GB_OP_XOR || op > GB_OP_MERGE || nA < 0 || nB < 0 || out_cap < 0 || !d_out || !d_count ||
+      (nA && !d_A) || (nB && !d_B))
+    return na_refuse(GB_ERR_ARG, d_count, d_area, s);
   if ((long long)nA + nB > GB_NA_MAX_IN) {
     fprintf(stderr, "gb_bool_tile_noalloc: %lld input boxes exceed the static limit of %d\n",
             (long long)nA + nB, GB_NA_MAX_IN);
-    return GB_ERR_CAPACITY;
+    return na_refuse(GB_ERR_CAPACITY, d_count, d_area, s);
   }
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= GB_NA_MAX_DEV) return GB_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= GB_NA_MAX_DEV)
+    return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
   NoAllocState* S;
   char* scr;
   {
@@ -1152,30 +1185,52 @@ extern "C" int gb_bool_tile_noalloc(int op, const int4* d_A, int nA, const int4*
       if (cudaGetSymbolAddress(&a, g_na_state) != cudaSuccess ||
           cudaGetSymbolAddress(&b, g_na_scratch) != cudaSuccess) {
         fprintf(stderr, "gb_bool_tile_noalloc: cudaGetSymbolAddress failed on device %d\n", dev);
-        return GB_ERR_CUDA;
+        return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
       }
       if (cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)) !=
           cudaSuccess)
-        return GB_ERR_CUDA;
+        return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
       g_na_state_ptr[dev] = (NoAllocState*)a;
       g_na_scratch_ptr[dev] = (char*)b;
     }
     S = g_na_state_ptr[dev];
     scr = g_na_scratch_ptr[dev];
   }
-  cudaStream_t s = (cudaStream_t)stream;
+  // each launch reports its own error (no reliance on the thread's last-error state)
   const int g = 16;
-  k_na_prep<<<1, 256, 0, s>>>(S, op, d_A, nA, d_B, nB, g);
-  k_tile<<<1, TK_NT, sizeof(TileSmem), s>>>(op, &S->L[0], &S->L[1], &S->L[2], g, 0, scr, GB_NA_SCRATCH, S->ctr,
-                                            &S->st);
-  k_na_export<<<8, 256, 0, s>>>(S, d_out, out_cap, d_count, d_area);
-  if (cudaGetLastError() != cudaSuccess) return GB_ERR_CUDA;
-  DStatus hs;
-  if (cudaMemcpyAsync(&hs, &S->st, sizeof(hs), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+  {
+    void* args[] = {&S, &op, &d_A, &nA, &d_B, &nB, (void*)&g};
+    if (cudaLaunchKernel((const void*)k_na_prep, dim3(1), dim3(256), args, 0, s) != cudaSuccess)
+      return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
+  }
+  {
+    DLayer* la = &S->L[0];
+    DLayer* lb = &S->L[1];
+    DLayer* lo = &S->L[2];
+    int gg = g, mode = 0;
+    unsigned long long scr_bytes = GB_NA_SCRATCH;
+    long long* ctr = S->ctr;
+    DStatus* st = &S->res.st;
+    void* args[] = {&op, &la, &lb, &lo, &gg, &mode, &scr, &scr_bytes, &ctr, &st};
+    if (cudaLaunchKernel((const void*)k_tile, dim3(1), dim3(TK_NT), args, sizeof(TileSmem), s) != cudaSuccess)
+      return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
+  }
+  {
+    void* args[] = {&S, &d_out, &out_cap, &d_count, &d_area};
+    if (cudaLaunchKernel((const void*)k_na_export, dim3(8), dim3(256), args, 0, s) != cudaSuccess)
+      return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
+  }
+  NoAllocResult hr;
+  if (cudaMemcpyAsync(&hr, &S->res, sizeof(hr), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return GB_ERR_CUDA;
-  if (hs.err == GB_ERR_CAPACITY)
+  if (hr.st.err == GB_ERR_CAPACITY)
     fprintf(stderr, "gb_bool_tile_noalloc: result exceeds the static limits (%d strips, %u scratch bytes)\n",
             GB_NA_MAX_OUT, GB_NA_SCRATCH);
-  return hs.err;
+  if (hr.st.err) return hr.st.err;
+  if (hr.nout > out_cap) {
+    fprintf(stderr, "gb_bool_tile_noalloc: %lld result strips exceed out_cap %lld\n", hr.nout, out_cap);
+    return GB_ERR_CAPACITY;
+  }
+  return GB_OK;
 }
