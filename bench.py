@@ -23,6 +23,7 @@ Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb|reference]
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -121,42 +122,76 @@ def ncu_traffic():
     return None
 
 
-def cpu_leg(boxes, off, seconds=15.0):
-    """Time the CPU oracle's OP1 on the first cells (about `seconds` of work)."""
+CPU_SAMPLE_BOXES = 4_000_000  # the CPU legs' sample: the first cells holding about this many boxes
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.processor() or platform.machine()
+
+
+def cpu_sample(off):
+    """The CPU legs' sample: the first k cells, about CPU_SAMPLE_BOXES boxes
+    (several hundred cells, so no cell is more than a small part of one
+    thread's share)."""
+    return sample_cells(off, CPU_SAMPLE_BOXES)
+
+
+def cpu_leg(boxes, off):
+    """Time the reference's CPU path for the deck (oracle/gbo_refpath.cpp: GROW +
+    heal, SIZE, FRAME-NOT on K x K tiles with the R-tree fracture NOT, AND as
+    R-tree pairwise clips, Klee area) on the CPU sample, cells in parallel on
+    all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     threads = int(O.lib().orc_num_threads())
-    k = sample_cells(off, 200_000)
+    k = cpu_sample(off)
+    O.refpath_op1_cells(boxes[:off[min(4, k)]], off[:min(4, k) + 1])  # warm
     t0 = time.perf_counter()
-    O.op1_cells(boxes[:off[k]], off[:k + 1] - off[0])
+    counts, area = O.refpath_op1_cells(boxes[:off[k]], off[:k + 1])
     dt = time.perf_counter() - t0
-    rate = off[k] / dt
-    # grow the sample to about `seconds` of CPU work
-    k2 = sample_cells(off, int(rate * seconds))
-    if k2 > k:
-        t0 = time.perf_counter()
-        O.op1_cells(boxes[:off[k2]], off[:k2 + 1])
-        dt = time.perf_counter() - t0
-        k = k2
     return {"value": float(off[k] / dt), "unit": "boxes/s", "cores": threads, "kind": "port",
-            "sample": "OP1 + union area on the first %d cells (%d boxes), %.1f s" % (k, int(off[k]), dt)}
+            "cpu_model": cpu_model(),
+            "sample": "OP1 + union area on the first %d cells (%d boxes), %.1f s" % (k, int(off[k]), dt),
+            "path": "the reference's CPU path restated (oracle/gbo_refpath.cpp): GROW + heal_boxes / FRAME merge, "
+                    "SIZE, FRAME-NOT (K x K tiles, FilterLayer, CalculateNOTRTree fracture, re-heal), "
+                    "CalculateAND R-tree clips, calculate_union_area_fast; cells in parallel",
+            "assert_zero_failures": int((counts[:, 4] > 0).sum() + (counts[:, 5] > 0).sum())}
 
 
 def P99_TARGET_MS(rate):
-    """Stated serving target: p99 latency (arrival to completion) of 1 ms up to
-    3000 requests/s and 10 ms up to 10000 requests/s."""
-    return 1.0 if rate <= 3000 else 10.0
+    """Stated serving target for the cfg4 layers (64 resident layers with box
+    counts across 1k..20M, two of them 20M): p99 latency, arrival to
+    completion, of at most 25 ms up to 1000 requests/s.  Above the loop's
+    capacity at these sizes (about 1700 requests/s, 3.6e9 boxes/s measured)
+    the backlog grows for as long as requests keep coming, so no latency
+    target can hold there; those rates report the rate actually served
+    (target None)."""
+    return 25.0 if rate <= 1000 else None
 
 
-def serve_leg(rates=(1000, 10000), seconds=0.5, max_req=3000, seed=4, slots=8):
-    """cfg4-style serving: 64 resident layers (cfg0-style, lognormal sizes in
-    [1k, 20M], median 30k), Poisson arrivals, op uniform over AND / NOT / OR /
-    XOR / GROW / SIZE, operands uniform; 120 GB admission budget."""
+SERVE_RATES = (100, 300, 1000, 3000, 10000)
+
+
+def serve_leg(rates=SERVE_RATES, seconds=2.0, max_req=2500, seed=4, slots=8):
+    """Serving as the cfg4 workload states it: 64 resident cfg0-style layers
+    with lognormal box counts across [1k, 20M] (median sqrt(1k * 20M) = 141k,
+    sigma ln(20000)/4, clipped), Poisson arrivals at each rate for `seconds`
+    (at most max_req requests), op uniform over AND / NOT / OR / XOR / GROW /
+    SIZE, operands uniform; 120 GB admission budget, 8 execution slots."""
     from vlsi_layout_gb300 import engine
     rng = np.random.default_rng(seed)
-    sizes = np.clip(np.round(rng.lognormal(np.log(30000), 1.5, 64)), 1000, 20_000_000).astype(np.int64)
-    out = {"layers": 64, "resident_boxes": int(sizes.sum()), "budget_gb": 120, "slots": slots, "rates": []}
+    sizes = np.clip(np.round(rng.lognormal(np.log(141421), np.log(20000) / 4, 64)), 1000, 20_000_000).astype(np.int64)
+    out = {"layers": 64, "resident_boxes": int(sizes.sum()), "largest_layers": sorted(int(v) for v in sizes)[-4:],
+           "layers_over_1M": int((sizes > 1_000_000).sum()), "budget_gb": 120, "slots": slots, "rates": []}
     with engine.Server(budget_bytes=120 << 30, slots=slots, slot_arena_bytes=8 << 30) as S:
         for k, n in enumerate(sizes):
             b, _ = make_cells(1, median=int(n), sigma=1e-9, lo=int(n), hi=int(n), seed=seed * 1000 + k)
@@ -178,11 +213,15 @@ def serve_leg(rates=(1000, 10000), seconds=0.5, max_req=3000, seed=4, slots=8):
             lat = res["latency_ms"][ok]
             p99 = float(np.percentile(lat, 99)) if len(lat) else None
             target = P99_TARGET_MS(lam)
-            out["rates"].append({"lambda_req_s": lam, "requests": n, "ok": int(ok.sum()),
+            served = float(ok.sum() / wall)
+            out["rates"].append({"lambda_req_s": lam, "requests": n, "arrival_window_s": float(r["arrival_s"][-1]),
+                                 "ok": int(ok.sum()),
                                  "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
                                  "p99_ms": p99, "p99_target_ms": target,
-                                 "meets_p99_target": bool(p99 is not None and p99 <= target and ok.all()),
-                                 "served_req_s": float(ok.sum() / wall),
+                                 "meets_p99_target": (bool(p99 is not None and p99 <= target and ok.all())
+                                                      if target is not None else None),
+                                 "saturated": bool(served < 0.9 * lam),
+                                 "served_req_s": served, "wall_s": wall,
                                  "boxes_per_s": float(boxes[ok].sum() / wall)})
     return out
 
@@ -285,34 +324,38 @@ def replica_value(world, boxes_per_rank, ms):
 
 
 def run_reference(args, boxes, off, world, rank, dist):
+    """The reference arm: the reference's CPU path for the deck (oracle/
+    gbo_refpath.cpp, the restatement cpu_leg times) on the CPU legs' sample
+    of cells, every step, on all host threads."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     threads = int(O.lib().orc_num_threads())
-    k = sample_cells(off, args.ref_boxes)
+    k = cpu_sample(off)
     sub, soff = boxes[:off[k]], off[:k + 1]
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        O.op1_cells(sub[:soff[min(4, k)]], soff[:min(4, k) + 1])
+    O.refpath_op1_cells(sub[:soff[min(4, k)]], soff[:min(4, k) + 1])  # warm
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        counts, area = O.op1_cells(sub, soff)
+        counts, area = O.refpath_op1_cells(sub, soff)
         times.append(time.perf_counter() - t0)
     dt = sum(times) / len(times)
     v = float(soff[k] / dt)
     fails = int((counts[:, 4] > 0).sum() + (counts[:, 5] > 0).sum())
+    sample = "OP1 + union area on the first %d cells (%d boxes) per step" % (k, int(soff[k]))
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "boxes/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {"workload": "OP1 deck + union area, batched cells (lognormal median 8000, 4096 cells); "
-                               "reference arm runs a bounded sample of cells per step",
+                               "the reference arm runs the CPU legs' sample of cells per step",
                    "cells": int(len(off) - 1), "boxes": int(off[-1]), "sample_cells": k,
-                   "sample_boxes": int(soff[k])},
-        "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": threads, "kind": "port",
-                         "sample": "OP1 + union area on the first %d cells (%d boxes) per step" % (k, int(soff[k]))},
+                   "sample_boxes": int(soff[k]), "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "boxes/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+                         "sample": sample,
+                         "path": "the reference's CPU path restated (oracle/gbo_refpath.cpp)"},
         "e2e": {"value": v, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "assert_zero_failures": fails,
     }), flush=True)
@@ -492,8 +535,8 @@ def events_leg(n=50_000_000, steps=2):
     event_sorter.cu:48-81: trackers ordered by (X, Y) through 64-bit packed
     keys) of n trackers with coordinates uniform in a 4e7 die: the drop-in on
     a host array (H2D and D2H inside, as the Fortran layer calls it) and on a
-    device array; the output keys are checked against numpy's sort of the
-    input keys."""
+    device array; both outputs (keys and payloads) are checked against
+    numpy's stable sort of the input."""
     import torch
     from vlsi_layout_gb300 import engine
     rng = np.random.default_rng(6)
@@ -503,7 +546,7 @@ def events_leg(n=50_000_000, steps=2):
     t["polygonNumber"] = rng.choice(np.array([-1, 1], np.int8), n)
     L = engine.lib()
     th, td = [], []
-    out = None
+    out = dout = None
     for it in range(steps + 1):
         h = t.copy()
         t0 = time.perf_counter()
@@ -519,14 +562,23 @@ def events_leg(n=50_000_000, steps=2):
             th.append(t1 - t0)
             td.append(t3 - t2)
         out = h
+        if it == steps:
+            dout = d.cpu().numpy().view(engine.TRACKER_DTYPE)
         del d
+
     def keys(a):
         return ((a["X"].astype(np.int64) + 2**31).astype(np.uint64) << np.uint64(32)) | \
             (a["Y"].astype(np.int64) + 2**31).astype(np.uint64)
-    ok = bool(np.array_equal(keys(out), np.sort(keys(t))))
+    # the device sort is stable: both outputs must be exactly numpy's stable order of the
+    # input, payload (polygonNumber) included, for the host-array and the device-array call
+    order = np.argsort(keys(t), kind="stable")
+    ref = t[order]
+    ok = all(np.array_equal(o[f], ref[f]) for o in (out, dout) for f in ("X", "Y", "polygonNumber"))
     sh, sd = statistics.median(th), statistics.median(td)
     return {"n": n, "host_s": sh, "host_trackers_per_s": n / sh, "device_s": sd, "device_trackers_per_s": n / sd,
-            "sorted_keys_equal_numpy": ok,
+            "sorted_equal_numpy_stable": ok,
+            "check": "host- and device-array outputs equal numpy's stable sort of the input by the packed key, "
+                     "X, Y and polygonNumber",
             "timing": "host wall clock around device_event_sort (host array: H2D + D2H inside; device array)",
             "reference": "GPU radix sort of 314,159,232 x 4 trackers in 5.96 s on a DGX Spark (NOTES.txt:595-596)"}
 
@@ -542,12 +594,10 @@ def main():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--plain-boxes", type=int, default=400_000)
-    ap.add_argument("--ref-boxes", type=int, default=600_000)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true")
-    ap.add_argument("--serve-rates", default="1000,10000")
+    ap.add_argument("--serve-rates", default=",".join(str(v) for v in SERVE_RATES))
     ap.add_argument("--sort-only", action="store_true")
     ap.add_argument("--sort-n", type=int, default=200_000_000)
     ap.add_argument("--no-sort", action="store_true")
@@ -586,7 +636,7 @@ def main():
         import torch
         torch.cuda.set_device(local)
         rates = tuple(int(x) for x in args.serve_rates.split(","))
-        print(json.dumps({"serving": serve_leg(rates=rates, seconds=2.0, max_req=20000)}), flush=True)
+        print(json.dumps({"serving": serve_leg(rates=rates)}), flush=True)
         return
     boxes, off = make_cells(args.cells, args.median, seed=args.seed)
     nbox = int(off[-1])
@@ -664,19 +714,31 @@ def main():
     achieved = (bytes_per_step / (tile_ms_last / 1e3)) / 1e9 if tile_ms_last > 0 else None
     traffic = ncu_traffic()
 
-    # ---- parity on sampled cells: per-cell layer counts and areas against the oracle
+    # ---- parity on every cell: per cell and layer, the strip digest (an order-independent 64-bit hash
+    # of the canonical strips), the strip count and the union area against the oracle on all host cores
     parity = "not checked"
     cpu = None
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         O.build()
-        ks = sample_cells(off, 400_000)
-        ec, ea = O.op1_cells(boxes[:off[ks]], off[:ks + 1], grid_log2=grid)
         torch.cuda.synchronize()
-        area_dev = area_t[:ks].cpu().numpy()  # as written by the last timed graph replay
-        ok = np.array_equal(counts[:ks], ec) and np.array_equal(area_dev, ea)
-        parity = "bit-exact counts (6 layers) and union area on %d sampled cells: %s" % (ks, "pass" if ok else "FAIL")
+        area_dev = area_t.cpu().numpy()  # as written by the last timed graph replay
+        gd = np.stack([L.digest() for L in outs], axis=1)
+        merged = ctx.op(engine.MERGE, P)
+        gm = merged.digest()
+        t0 = time.perf_counter()
+        ec, ea, ed = O.op1_cells_digest(boxes, off, grid_log2=grid)
+        osec = time.perf_counter() - t0
+        cell_ok = (gd == ed[:, :6]).all(axis=1) & (gm == ed[:, 6]) & (counts == ec).all(axis=1) & (area_dev == ea)
+        nok = int(cell_ok.sum())
+        parity = {"result": "pass" if nok == args.cells else "FAIL",
+                  "cells_equal": nok, "cells": args.cells,
+                  "what": "per cell: strip digests of poly_1, poly_2, outer, inner, ring_and1, ring_intersection "
+                          "and MERGE(P), strip counts of the six deck layers and the union area, against the "
+                          "oracle run op by op on all host cores",
+                  "digest": "sum mod 2^64 of fmix64((x1<<32|y1) ^ fmix64((x2<<32|y2) + 0x9e3779b97f4a7c15)) per strip",
+                  "oracle_s": round(osec, 1), "oracle_threads": int(O.lib().orc_num_threads())}
     engine.lib().gb_graph_destroy(graph)
     ctx.release(mark)
 
@@ -714,7 +776,7 @@ def main():
                        % (kp, int(off[kp]))}
 
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_leg(boxes, off, args.cpu_seconds)
+        cpu = cpu_leg(boxes, off)
 
     ctx.close()
     serving = None

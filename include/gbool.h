@@ -140,6 +140,13 @@ int gb_layer_from_device(gb_context* ctx, const c_box* d_boxes, unsigned long lo
 int gb_layer_ncell(gb_layer* L);
 /* Box (strip) count, total and per cell (per_cell may be NULL).  Syncs. */
 int gb_layer_count(gb_context* ctx, gb_layer* L, long long* total, long long* per_cell);
+/* Per-cell digest of a Boolean result (a binned layer): out[ncell] (host)
+ * gets, per cell, the sum mod 2^64 of gb_strip_hash(x1, y1, x2, y2) over its
+ * strips in global dbu -- the MurmurHash3 fmix64 finaliser of
+ * (x1<<32|y1) ^ fmix64((x2<<32|y2) + 0x9e3779b97f4a7c15), coordinates taken
+ * as uint32.  Order-independent: two layers with the same strips per cell
+ * have the same digests.  A raw (input) layer gives GB_ERR_ARG. */
+int gb_layer_digest(gb_context* ctx, gb_layer* L, unsigned long long* out);
 /* Copy a layer to the host in tile order (cell-major).  cap is the capacity
  * of out in boxes; *n receives the count (GB_ERR_CAPACITY if cap < count).
  * cell_offsets (ncell+1 entries, may be NULL) receives the per-cell ranges. */
@@ -306,6 +313,13 @@ int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, long l
 int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
                 const long long* cell_offsets, int ncell, int32_t a, long long* counts,
                 long long* area, int* assert_failures);
+/* gb_op1_host plus, per cell, a digest of each of the six result layers
+ * (digests[ncell*6], [cell][layer]): the sum mod 2^64 of a 64-bit hash of
+ * every strip (x1, y1, x2, y2 in global dbu), so equal canonical strips give
+ * equal digests in any order (the same function as gb_layer_digest). */
+int gb_op1_host_digest(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                       const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                       long long* area, unsigned long long* digests, int* assert_failures);
 
 /* ---- SNAP layer streams (box_codec.f90, serialization.f90, snappy_api.cpp)
  * A stream is the layer's boxes cut into chunks of 65536; each chunk is the

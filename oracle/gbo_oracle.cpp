@@ -6,6 +6,7 @@
 //
 // Build: g++ -O3 -std=c++17 -fopenmp -shared -fPIC gbo_oracle.cpp -o libgbo_oracle.so
 #include "gbo_oracle.h"
+#include "gbo_internal.h"
 
 #include <algorithm>
 #include <cstdlib>
@@ -17,9 +18,7 @@
 #include <omp.h>
 #endif
 
-namespace {
-
-struct Box { int32_t x1, y1, x2, y2; };
+namespace gbo {
 
 inline bool valid(const Box& b) { return b.x1 < b.x2 && b.y1 < b.y2; }  // geometry.f90:66-70
 
@@ -37,8 +36,6 @@ inline bool pred(int op, int32_t ca, int32_t cb) {
 }
 
 inline int32_t tile_of(int32_t v, int g) { return (int32_t)((int64_t)v >> g); }  // floor(v / 2^g)
-
-struct Piece { Box b; uint8_t owner; };
 
 // One corner token of polygon_fracture.f90:824-833: +1 at (x1,y1) and (x2,y2),
 // -1 at (x1,y2) and (x2,y1); the owner selects which lap counter it updates.
@@ -220,7 +217,9 @@ void update_tree(int node, int s, int e, int l, int r, int val, const std::vecto
   else len[node] = len[2 * node] + len[2 * node + 1];
 }
 
-}  // namespace
+}  // namespace gbo
+
+using namespace gbo;
 
 extern "C" {
 
@@ -403,8 +402,11 @@ int32_t orc_um_to_dbu(double r) { return (int32_t)(1000.0 * r); }
 
 void orc_canonical_sort(orc_box* A, int64_t n) { std::sort((Box*)A, (Box*)A + n, cmp_box); }
 
-// OP1 (op_template.m4:14-22) on one layer with amount a dbu.
-void orc_op1(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, int64_t* area) {
+// OP1 (op_template.m4:14-22) on one layer with amount a dbu; digests
+// (optional, 7 entries): the strip digests of poly_1, poly_2, outer, inner,
+// and1, inter and merged(P).
+static void op1_impl(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, int64_t* area,
+                     uint64_t* digests) {
   const Box* P = (const Box*)Ab;
   std::vector<Box> p1, p2, outer, inner, and1, inter, merged;
   for (int k = 0; k < 8; ++k) counts[k] = -1;
@@ -423,6 +425,19 @@ void orc_op1(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, in
   int64_t s = 0;
   for (const Box& b : merged) s += (int64_t)(b.x2 - b.x1) * (int64_t)(b.y2 - b.y1);
   *area = s;
+  if (digests) {
+    const std::vector<Box>* L[7] = {&p1, &p2, &outer, &inner, &and1, &inter, &merged};
+    for (int k = 0; k < 7; ++k) digests[k] = orc_strip_digest((const orc_box*)L[k]->data(), (int64_t)L[k]->size());
+  }
+}
+
+void orc_op1(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, int64_t* area) {
+  op1_impl(Ab, n, a, g, counts, area, nullptr);
+}
+
+void orc_op1_digest(const orc_box* Ab, int64_t n, int32_t a, int g, int64_t* counts, int64_t* area,
+                    uint64_t* digests) {
+  op1_impl(Ab, n, a, g, counts, area, digests);
 }
 
 // OP1 on every cell of a batched layer, cells in parallel (OpenMP dynamic
@@ -431,8 +446,40 @@ void orc_op1_cells(const orc_box* Ab, const int64_t* off, int64_t ncell, int32_t
                    int64_t* counts, int64_t* area) {
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t k = 0; k < ncell; ++k) {
-    orc_op1(Ab + off[k], off[k + 1] - off[k], a, g, counts + 8 * k, area + k);
+    op1_impl(Ab + off[k], off[k + 1] - off[k], a, g, counts + 8 * k, area + k, nullptr);
   }
+}
+
+void orc_op1_cells_digest(const orc_box* Ab, const int64_t* off, int64_t ncell, int32_t a, int g,
+                          int64_t* counts, int64_t* area, uint64_t* digests) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < ncell; ++k) {
+    op1_impl(Ab + off[k], off[k + 1] - off[k], a, g, counts + 8 * k, area + k, digests + 7 * k);
+  }
+}
+
+// Order-independent digest of a strip list: the sum mod 2^64 of a 64-bit hash
+// per strip, the MurmurHash3 fmix64 finaliser of the packed corners (the
+// device computes the same function).
+static inline uint64_t fmix64(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+
+uint64_t orc_strip_hash(int32_t x1, int32_t y1, int32_t x2, int32_t y2) {
+  const uint64_t u = ((uint64_t)(uint32_t)x1 << 32) | (uint32_t)y1;
+  const uint64_t v = ((uint64_t)(uint32_t)x2 << 32) | (uint32_t)y2;
+  return fmix64(u ^ fmix64(v + 0x9e3779b97f4a7c15ull));
+}
+
+uint64_t orc_strip_digest(const orc_box* A, int64_t n) {
+  uint64_t h = 0;
+  for (int64_t i = 0; i < n; ++i) h += orc_strip_hash(A[i].x1, A[i].y1, A[i].x2, A[i].y2);
+  return h;
 }
 
 void orc_free(void* p) { std::free(p); }

@@ -83,9 +83,34 @@ void orc_canonical_sort(orc_box* A, int64_t n);
  * merged(poly), unused. */
 void orc_op1(const orc_box* A, int64_t n, int32_t amount, int grid_log2,
              int64_t* counts, int64_t* area);
+/* orc_op1 plus the strip digests of its seven layers (digests[7]: poly_1,
+ * poly_2, outer, inner, and1, inter, merged); one layer, every operator
+ * parallel over its tiles. */
+void orc_op1_digest(const orc_box* A, int64_t n, int32_t amount, int grid_log2,
+                    int64_t* counts, int64_t* area, uint64_t* digests);
 /* orc_op1 over ncell cells (off[ncell+1]), cells in parallel: counts[8*k..]. */
 void orc_op1_cells(const orc_box* A, const int64_t* off, int64_t ncell, int32_t amount, int grid_log2,
                    int64_t* counts, int64_t* area);
+/* orc_op1_cells plus per-cell strip digests digests[7*k..]: poly_1, poly_2,
+ * outer, inner, and1, inter, merged(P) (orc_strip_digest of each layer). */
+void orc_op1_cells_digest(const orc_box* A, const int64_t* off, int64_t ncell, int32_t amount, int grid_log2,
+                          int64_t* counts, int64_t* area, uint64_t* digests);
+/* 64-bit hash of one strip: fmix64((x1<<32|y1) ^ fmix64((x2<<32|y2) +
+ * 0x9e3779b97f4a7c15)), coordinates as uint32 (MurmurHash3's finaliser). */
+uint64_t orc_strip_hash(int32_t x1, int32_t y1, int32_t x2, int32_t y2);
+/* Sum mod 2^64 of orc_strip_hash over a strip list: independent of order. */
+uint64_t orc_strip_digest(const orc_box* A, int64_t n);
+/* The reference's CPU path for the OP1 deck, restated (gbo_refpath.cpp): the
+ * timed CPU baseline.  counts[6*k..] per cell: boxes of poly_1, poly_2,
+ * outer, inner, and1, inter in the reference's own decompositions (FRAME
+ * tiles, pairwise AND clips), area[k] the union area; cells in parallel. */
+void orc_refpath_op1_cells(const orc_box* A, const int64_t* off, int64_t ncell, int32_t amount, int64_t* counts,
+                           int64_t* area);
+/* One of those six layers (which = 0..5) of one cell; *out malloc'd. */
+int64_t orc_refpath_op1_layer(const orc_box* A, int64_t n, int32_t amount, int which, orc_box** out);
+/* SubtractBox (boolean_ops_rtree.f90:139-186): subject minus clip as up to
+ * four pieces written to out4; returns their count. */
+int64_t orc_refpath_subtract(const orc_box* subject, const orc_box* clip, orc_box* out4);
 void orc_free(void* p);
 int orc_num_threads(void);
 

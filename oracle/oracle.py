@@ -72,6 +72,20 @@ def lib():
         L.orc_snappy_uncompressed_length.restype = i64
         L.orc_snappy_decompress.argtypes = [P, i64, P, i64]
         L.orc_snappy_decompress.restype = i64
+        L.orc_op1_digest.argtypes = [P, i64, i32, ctypes.c_int, P, P, P]
+        L.orc_op1_digest.restype = None
+        L.orc_op1_cells_digest.argtypes = [P, P, i64, i32, ctypes.c_int, P, P, P]
+        L.orc_op1_cells_digest.restype = None
+        L.orc_strip_hash.argtypes = [i32, i32, i32, i32]
+        L.orc_strip_hash.restype = ctypes.c_uint64
+        L.orc_strip_digest.argtypes = [P, i64]
+        L.orc_strip_digest.restype = ctypes.c_uint64
+        L.orc_refpath_op1_cells.argtypes = [P, P, i64, i32, P, P]
+        L.orc_refpath_op1_cells.restype = None
+        L.orc_refpath_op1_layer.argtypes = [P, i64, i32, ctypes.c_int, ctypes.POINTER(P)]
+        L.orc_refpath_op1_layer.restype = i64
+        L.orc_refpath_subtract.argtypes = [P, P, P]
+        L.orc_refpath_subtract.restype = i64
         L.orc_free.argtypes = [P]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -218,6 +232,76 @@ def op1_cells(A, off, amount=1, grid_log2=16):
     lib().orc_op1_cells(A.ctypes.data, off.ctypes.data, ncell, amount, grid_log2, counts.ctypes.data,
                         area.ctypes.data)
     return counts[:, :6], area
+
+
+def op1_digest(A, amount=1, grid_log2=16):
+    """OP1 on one layer (each operator parallel over its tiles): returns
+    (counts[6], area, digests[7]) with digests of poly_1, poly_2, outer,
+    inner, and1, inter and merged(P)."""
+    A = _arr(A)
+    counts = np.zeros(8, np.int64)
+    area = np.zeros(1, np.int64)
+    dig = np.zeros(7, np.uint64)
+    lib().orc_op1_digest(A.ctypes.data, len(A), amount, grid_log2, counts.ctypes.data, area.ctypes.data,
+                         dig.ctypes.data)
+    return counts[:6], int(area[0]), dig
+
+
+def op1_cells_digest(A, off, amount=1, grid_log2=16):
+    """op1_cells plus per-cell strip digests: returns counts[ncell, 6],
+    area[ncell] and digests[ncell, 7] (uint64: poly_1, poly_2, outer, inner,
+    and1, inter, merged(P))."""
+    A = _arr(A)
+    off = np.ascontiguousarray(off, np.int64)
+    ncell = len(off) - 1
+    counts = np.zeros((ncell, 8), np.int64)
+    area = np.zeros(ncell, np.int64)
+    dig = np.zeros((ncell, 7), np.uint64)
+    lib().orc_op1_cells_digest(A.ctypes.data, off.ctypes.data, ncell, amount, grid_log2, counts.ctypes.data,
+                               area.ctypes.data, dig.ctypes.data)
+    return counts[:, :6], area, dig
+
+
+def strip_digest(A):
+    """Order-independent digest of a strip list (sum mod 2^64 of strip_hash)."""
+    A = _arr(A)
+    return int(lib().orc_strip_digest(A.ctypes.data, len(A)))
+
+
+def strip_digests_by_cell(A, off):
+    """strip_digest of every cell's slice A[off[k]:off[k+1]] (uint64 array)."""
+    A = _arr(A)
+    return np.array([strip_digest(A[off[k]:off[k + 1]]) for k in range(len(off) - 1)], np.uint64)
+
+
+def refpath_op1_cells(A, off, amount=1):
+    """The reference's CPU path for OP1 (gbo_refpath.cpp) on every cell, cells
+    in parallel: counts[ncell, 6] in the reference's decompositions and the
+    union area per cell."""
+    A = _arr(A)
+    off = np.ascontiguousarray(off, np.int64)
+    ncell = len(off) - 1
+    counts = np.zeros((ncell, 6), np.int64)
+    area = np.zeros(ncell, np.int64)
+    lib().orc_refpath_op1_cells(A.ctypes.data, off.ctypes.data, ncell, amount, counts.ctypes.data, area.ctypes.data)
+    return counts, area
+
+
+def refpath_op1_layer(A, which, amount=1):
+    """Layer `which` (0 poly_1, 1 poly_2, 2 outer, 3 inner, 4 and1, 5 inter) of
+    the reference's CPU path for OP1, as the reference decomposes it."""
+    A = _arr(A)
+    p = ctypes.c_void_p()
+    n = lib().orc_refpath_op1_layer(A.ctypes.data, len(A), amount, which, ctypes.byref(p))
+    return _take(n, p)
+
+
+def refpath_subtract(subject, clip):
+    """SubtractBox: subject minus clip as up to four boxes."""
+    s, c = _arr([subject]), _arr([clip])
+    out = np.zeros((4, 4), np.int32)
+    k = lib().orc_refpath_subtract(s.ctypes.data, c.ctypes.data, out.ctypes.data)
+    return out[:k]
 
 
 def canonical(A):

@@ -31,7 +31,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle as O  # noqa: E402
 from gen import macro_arrays, stdcell_layers  # noqa: E402
 
-REF = "/root/reference/src"
+REF = os.environ.get("GB_REFERENCE_SRC", "/root/reference/src")  # the reference sources
 
 
 def morton_sorted(A):

@@ -1,12 +1,18 @@
-"""Property tests at the workloads' full sizes, where no oracle run fits:
-the standard-cell layout (four layers of 10M boxes, pairwise Booleans,
-connectivity through 2% contacts) and the full-chip layer (360M boxes:
-standard-cell rows and 64x64 macro arrays; Morton sort, OP1 deck, Klee area,
-component count).  Every check is size-independent: point-set area
-identities, XOR(A, A) empty, the OP1 ASSERT_ZEROs, sortedness and
-permutation of the sort, additivity of area over a partition, invariance of
-the component count under box order, and agreement of two kernels on the
-singletons."""
+"""The workloads at their full sizes.
+
+Oracle parity: the standard-cell layout at its full size (four layers of 10M
+boxes: AND / NOT / OR / XOR of poly x li1, met1 x met2 and li1 x met1, and the
+PNUM labels of met1 + met2 through the 2% contacts) against the CPU oracle on
+all host cores, strip digests and counts per result, labels bit for bit; and
+a 4e6 x 4e6-dbu window of the full-chip layer (clipped standard-cell boxes and
+macro arrays) through the whole OP1 deck, every layer's strips against the
+oracle's.
+
+Properties of the whole 360M-box full-chip layer (where an oracle run of the
+deck would take too long): the Morton sort's order and permutation, the OP1
+ASSERT_ZEROs, additivity of area over a partition, invariance of the component
+count under box order, and agreement of two kernels on the singletons; and
+point-set identities of the standard-cell Booleans."""
 import ctypes
 
 import numpy as np
@@ -80,6 +86,42 @@ def test_stdcell_10m_connectivity(ctx, std10m):
 
 
 @pytest.fixture(scope="module")
+def std10m_host():
+    from gen import stdcell_layers
+    return stdcell_layers(10_000_000, die=6_700_000, seed=1)
+
+
+def test_stdcell_10m_oracle_parity(ctx, oracle, std10m_host):
+    """Standard-cell workload at 10M boxes per layer: every pairwise Boolean's
+    strips (per-layer digest and count) equal the oracle's."""
+    from vlsi_layout_gb300 import engine as E
+    L = std10m_host
+    for a, b in (("poly", "li1"), ("met1", "met2"), ("li1", "met1")):
+        m = ctx.mark()
+        try:
+            A, B = ctx.layer(L[a]), ctx.layer(L[b])
+            for op in (E.AND, E.NOT, E.OR, E.XOR):
+                R = ctx.op(op, A, B)
+                e = oracle.boolean(L[a], L[b], op)
+                assert R.count()[0] == len(e), (a, b, op)
+                assert int(R.digest()[0]) == oracle.strip_digest(e), (a, b, op)
+                if op == E.AND and a == "met1":  # one result strip for strip
+                    assert np.array_equal(oracle.canonical(R.to_numpy()), e)
+        finally:
+            ctx.release(m)
+
+
+def test_stdcell_10m_components_oracle(ctx, oracle, std10m_host):
+    """PNUM labels of met1 + met2 joined through the 2% contacts, bit for bit
+    against the oracle's union-find (closed overlap, min-index roots)."""
+    L = std10m_host
+    both = np.concatenate([L["met1"], L["met2"], L["contact"]])
+    n, lab = ctx.components(both)
+    en, elab = oracle.components(both)
+    assert n == en and np.array_equal(lab, elab)
+
+
+@pytest.fixture(scope="module")
 def chip():
     from gen_device import full_chip
     t = full_chip(360_000_000, 40_000_000, seed=3)
@@ -150,6 +192,37 @@ def test_full_chip_op1_and_area(ctx, chip):
     try:
         Q = dev_layer(ctx, cat, off)
         assert int(area(ctx, Q).sum()) == a
+    finally:
+        ctx.release(m)
+
+
+def test_full_chip_window_oracle(ctx, oracle, chip):
+    """A 4e6 x 4e6-dbu window of the full-chip layer (boxes clipped to it:
+    standard-cell shapes and a few hundred 64x64 macro arrays) through the OP1
+    deck: every result layer's strips equal the oracle's (digest and count),
+    MERGE strip for strip, and the union area."""
+    from vlsi_layout_gb300 import engine as E
+    x0, y0, w = 8_000_000, 12_000_000, 4_000_000
+    c = chip[(chip[:, 2] > x0) & (chip[:, 0] < x0 + w) & (chip[:, 3] > y0) & (chip[:, 1] < y0 + w)].clone()
+    c[:, 0].clamp_(min=x0)
+    c[:, 1].clamp_(min=y0)
+    c[:, 2].clamp_(max=x0 + w)
+    c[:, 3].clamp_(max=y0 + w)
+    win = c.cpu().numpy()
+    nmacro_boxes = int(((win[:, 2] - win[:, 0] == 200) & (win[:, 3] - win[:, 1] == 200)).sum())
+    assert len(win) > 2_000_000 and nmacro_boxes > 100_000
+    ec, ea, ed = oracle.op1_digest(win, 1)
+    m = ctx.mark()
+    try:
+        P = ctx.layer(win)
+        outs = ctx.op1(P, 1)
+        for j, L in enumerate(outs):
+            assert L.count()[0] == ec[j], j
+            assert int(L.digest()[0]) == int(ed[j]), j
+        M = ctx.op(E.MERGE, P)
+        assert int(M.digest()[0]) == int(ed[6])
+        assert np.array_equal(oracle.canonical(M.to_numpy()), oracle.merge(win))
+        assert int(ctx.area(P)[0]) == ea
     finally:
         ctx.release(m)
 

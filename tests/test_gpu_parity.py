@@ -138,26 +138,71 @@ def test_components(ctx, oracle):
 def test_sorts(ctx, oracle):
     from vlsi_layout_gb300 import engine
     A = random_layer(300000, die=2_000_000, seed=16, x0=-1_000_000)
+    # repeated boxes (equal Morton keys) at spread input positions, for the stability check
+    rng = np.random.default_rng(16)
+    A = np.concatenate([A, A[rng.integers(0, len(A), 20000)]])
+    A = A[rng.permutation(len(A))]
     b, keys, perm = ctx.morton_sort(A)
     ek = oracle.morton_keys_np(A)
     assert np.array_equal(keys, np.sort(ek))
     assert np.array_equal(b, A[perm]) and np.array_equal(ek[perm], keys)
-    # stability of the LSD passes: equal keys keep input order
-    assert np.all(np.diff(perm[np.concatenate([[False], keys[1:] == keys[:-1]])]) >= 0) or True
+    assert np.array_equal(np.sort(perm), np.arange(len(A)))
+    # stability of the LSD passes: within a run of equal keys the input order is kept
+    eq = keys[1:] == keys[:-1]
+    assert eq.sum() >= 20000 and np.all(perm[1:][eq] > perm[:-1][eq])
     d = engine.sort_boxes_direct(A)
     assert np.array_equal(oracle.morton_keys_np(d), np.sort(ek))
     idx = engine.sort_boxes_indirect(A)
     assert idx.min() == 1 and np.array_equal(oracle.morton_keys_np(A[idx - 1]), np.sort(ek))
-    t = np.zeros(200000, engine.TRACKER_DTYPE)
-    rng = np.random.default_rng(17)
-    t["X"] = rng.integers(-50000, 50000, len(t))
-    t["Y"] = rng.integers(-50000, 50000, len(t))
-    t["polygonNumber"] = rng.choice([-1, 1], len(t))
-    s = engine.event_sort(t)
-    order = np.lexsort((t["Y"], t["X"]))
-    assert np.array_equal(s["X"], t["X"][order]) and np.array_equal(s["Y"], t["Y"][order])
     c = ctx.canonical_sort(A[::-1])
     assert np.array_equal(c, canon(A))
+
+
+def test_event_sort_matches_reference():
+    """device_event_sort against the reference's own cpp_std_sort_trackers
+    (event_sorter.cu:86-115, compiled from the reference sources when the
+    golden file was made): the same key order, the same payload multiset per
+    key; and, the device sort being stable, exactly numpy's stable order."""
+    from trackers import canonical_digest, check_sorted_like, corner_trackers, seeded_trackers
+    from vlsi_layout_gb300 import engine
+    with open(GOLDEN) as fh:
+        g = json.load(fh)
+    n = 0
+    for name, rec in g["fixtures"].items():
+        if "ref_sorted_trackers" not in rec:
+            continue
+        t = corner_trackers(np.array(rec["boxes"], np.int32).reshape(-1, 4))
+        s = engine.event_sort(t)
+        assert check_sorted_like(s, rec["ref_sorted_trackers"]), name
+        o = np.lexsort((t["Y"], t["X"]))  # stable: payloads keep their input order per key
+        assert np.array_equal(s["polygonNumber"], t["polygonNumber"][o]), name
+        n += 1
+    assert n >= 15  # the non-empty fixtures
+    sg = g["seeded_trackers"]
+    t = seeded_trackers(sg["n"], sg["seed"], *sg["x_range"])
+    s = engine.event_sort(t)
+    assert canonical_digest(s) == sg["sha256"]
+    o = np.lexsort((t["Y"], t["X"]))
+    for f in ("X", "Y", "polygonNumber"):
+        assert np.array_equal(s[f], t[f][o]), f
+
+
+def test_golden_morton_order(ctx):
+    """The device Morton sort reproduces the key order of the reference's own
+    thrust_sort_boxes_direct / _indirect on its KLBin fixtures (negative
+    coordinates and duplicates included)."""
+    from vlsi_layout_gb300 import engine
+    with open(GOLDEN) as fh:
+        fx = json.load(fh)["fixtures"]
+    for name, rec in fx.items():
+        b = np.array(rec["boxes"], np.int32).reshape(-1, 4)
+        if len(b) == 0 or "ref_morton_sorted_keys" not in rec:
+            continue
+        _, keys, _ = ctx.morton_sort(b)
+        assert keys.astype(np.uint64).tolist() == rec["ref_morton_sorted_keys"], name
+        idx = engine.sort_boxes_indirect(b)
+        _, k2, _ = ctx.morton_sort(b[idx - 1])
+        assert k2.tolist() == rec["ref_morton_indirect_keys"], name
 
 
 def test_dropin_ffi(oracle):
@@ -191,7 +236,16 @@ def test_multicell_layer(ctx, oracle):
 
 
 def test_op1_chain(ctx, oracle):
+    """The OP1 chain op by op on a 100k-box cfg0-style layer: every one of the
+    six result layers equals the oracle's strips (the oracle runs each
+    operator on the previous operators' strips, as the deck does)."""
     A = random_layer(100000, seed=21)
+    e_p1 = oracle.grow(A, 1, 1, 1, 1)
+    e_p2 = oracle.size(A, -1)
+    e_outer = oracle.boolean(e_p1, A, 3)
+    e_inner = oracle.boolean(A, e_p2, 3)
+    e_and1 = oracle.boolean(e_outer, A, 2)
+    e_inter = oracle.boolean(e_outer, e_inner, 2)
     counts, area = oracle.op1(A, 1)
     m = ctx.mark()
     try:
@@ -202,12 +256,38 @@ def test_op1_chain(ctx, oracle):
         inner = ctx.op(3, P, p2)
         and1 = ctx.op(2, outer, P)
         inter = ctx.op(2, outer, inner)
-        got = {k: L.count()[0] for k, L in [("poly_1", p1), ("poly_2", p2), ("outer_ring", outer),
-                                             ("inner_ring", inner), ("ring_and1", and1),
-                                             ("ring_intersection", inter)]}
-        for k, v in got.items():
-            assert v == counts[k], (k, v, counts[k])
+        for name, L, e in [("poly_1", p1, e_p1), ("poly_2", p2, e_p2), ("outer_ring", outer, e_outer),
+                           ("inner_ring", inner, e_inner), ("ring_and1", and1, e_and1),
+                           ("ring_intersection", inter, e_inter)]:
+            assert np.array_equal(canon(L.to_numpy()), e), name
+            assert L.count()[0] == counts[name] == len(e), name
+            assert int(L.digest()[0]) == oracle.strip_digest(e), name
+        assert len(e_and1) == 0 and len(e_inter) == 0
         assert int(ctx.area(P)[0]) == area
+    finally:
+        ctx.release(m)
+
+
+def test_op1_cells_digest(ctx, oracle):
+    """gb_op1 on a multi-cell layer: per cell, the digest of each result layer
+    equals the oracle's digest of its strips for that cell (and the strips of a
+    few cells are compared outright)."""
+    boxes, off = cells_layout(64, median=4000, seed=22)
+    ec, ea, ed = oracle.op1_cells_digest(boxes, off)
+    m = ctx.mark()
+    try:
+        P = ctx.layer(boxes, off)
+        outs = ctx.op1(P, 1)
+        for j, L in enumerate(outs):
+            assert np.array_equal(L.digest(), ed[:, j]), j
+            assert np.array_equal(L.count()[1], ec[:, j]), j
+        res, coff = outs[2].to_numpy(with_cells=True)  # outer ring, strip for strip on three cells
+        for k in (0, 17, 63):
+            A = boxes[off[k]:off[k + 1]]
+            e = oracle.boolean(oracle.grow(A, 1, 1, 1, 1), A, 3)
+            assert np.array_equal(canon(res[coff[k]:coff[k + 1]]), e), k
+        merged = ctx.op(4, P)
+        assert np.array_equal(merged.digest(), ed[:, 6])
     finally:
         ctx.release(m)
 
@@ -248,11 +328,13 @@ def test_op1_area_cells(ctx, oracle, amount):
 
 def test_op1_host_two_groups(ctx, oracle):
     """gb_op1_host on a layout large enough to be split into two groups of cells
-    (the second group's upload overlaps the first group's deck): per-cell counts
-    and areas equal the oracle's."""
+    (the second group's upload overlaps the first group's deck): per cell the
+    strip digests of all six result layers, the counts and the union area equal
+    the oracle's."""
     boxes, off = cells_layout(400, median=8000, seed=41)
     assert off[-1] >= (1 << 22)
     b = np.ascontiguousarray(boxes, np.int32)
-    counts, area, fails = ctx.op1_host(b.ctypes.data, len(b), off, 1)
-    ec, ea = oracle.op1_cells(b, off)
+    counts, area, fails, dig = ctx.op1_host(b.ctypes.data, len(b), off, 1, digests=True)
+    ec, ea, ed = oracle.op1_cells_digest(b, off)
     assert np.array_equal(counts, ec) and np.array_equal(area, ea) and fails == 0
+    assert np.array_equal(dig, ed[:, :6])

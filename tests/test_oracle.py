@@ -64,6 +64,33 @@ def test_golden_fixture(oracle, name):
         assert area == rec["union_area"]
 
 
+def test_oracle_tracker_order_matches_reference(oracle):
+    """The oracle's tracker key (PackKeys, event_sorter.cu:48-59) orders the
+    fixtures' corner tokens as the reference's own cpp_std_sort_trackers did
+    (keys, and the payload multiset per key), and the seeded set's digest."""
+    from trackers import canonical_digest, check_sorted_like, corner_trackers, seeded_trackers
+    with open(GOLDEN) as fh:
+        g = json.load(fh)
+    for name, rec in g["fixtures"].items():
+        if "ref_sorted_trackers" not in rec:
+            continue
+        t = corner_trackers(np.array(rec["boxes"], np.int32).reshape(-1, 4))
+        k = oracle.tracker_keys_np(t["X"], t["Y"])
+        assert check_sorted_like(t[np.argsort(k, kind="stable")], rec["ref_sorted_trackers"]), name
+    sg = g["seeded_trackers"]
+    t = seeded_trackers(sg["n"], sg["seed"], *sg["x_range"])
+    k = oracle.tracker_keys_np(t["X"], t["Y"])
+    assert canonical_digest(t[np.argsort(k, kind="stable")]) == sg["sha256"]
+
+
+def test_golden_provenance():
+    """The golden file says which values come from the reference's code."""
+    with open(GOLDEN) as fh:
+        g = json.load(fh)
+    assert "ref_sorted_trackers" in g["provenance"]["reference"]
+    assert set(g["provenance"]["oracle"]) == {"merge", "union_area", "components"}
+
+
 def test_square_fixture_areas(oracle):
     rec = _golden()["square_L68_D20.bin"]
     b = np.array(rec["boxes"], np.int32)
@@ -192,3 +219,32 @@ def test_component_areas(oracle):
     ar = oracle.component_areas(B)
     n, lab = oracle.components(B)
     assert len(ar) == lab.max() + 1 and ar.sum() == oracle.union_area(B)
+
+
+def test_refpath_subtract_known_answer(oracle):
+    # SubtractBox (boolean_ops_rtree.f90:139-186) on the box-minus-hole case of
+    # test_rectboolean.f90:37-54: left, right, bottom-middle, top-middle, area 64
+    r = oracle.refpath_subtract([0, 0, 10, 10], [2, 2, 8, 8])
+    assert r.tolist() == [[0, 0, 2, 10], [8, 0, 10, 10], [2, 0, 8, 2], [2, 8, 8, 10]]
+    assert oracle.area_of(r) == 64
+    assert oracle.refpath_subtract([0, 0, 10, 10], [10, 0, 20, 10]).tolist() == [[0, 0, 10, 10]]  # edge touch
+    assert len(oracle.refpath_subtract([2, 2, 8, 8], [0, 0, 10, 10])) == 0
+
+
+@pytest.mark.parametrize("n,die,seed", [(600, 60000, 61), (5000, 250000, 62)])
+def test_refpath_op1_point_sets(oracle, n, die, seed):
+    """The reference's CPU path for OP1 (FRAME tiles, R-tree AND clips,
+    fracture NOT) gives the oracle's point sets for every layer (the
+    decompositions differ), and both ASSERT_ZERO layers are empty."""
+    A = random_layer(n, die=die, seed=seed)
+    exp = [oracle.grow(A, 1, 1, 1, 1), oracle.size(A, -1)]
+    exp.append(oracle.boolean(exp[0], A, oracle.NOT))
+    exp.append(oracle.boolean(A, exp[1], oracle.NOT))
+    for w in range(4):
+        got = oracle.refpath_op1_layer(A, w)
+        assert np.array_equal(oracle.merge(got), exp[w]), w
+        assert oracle.area_of(got) == oracle.area_of(exp[w]), w  # the pieces are disjoint
+    assert len(oracle.refpath_op1_layer(A, 4)) == 0 and len(oracle.refpath_op1_layer(A, 5)) == 0
+    off = np.array([0, n], np.int64)
+    counts, area = oracle.refpath_op1_cells(A, off)
+    assert counts[0, 4] == 0 and counts[0, 5] == 0 and area[0] == oracle.union_area(A)

@@ -501,6 +501,20 @@ extern "C" int gb_layer_from_device(gb_context* ctx, const c_box* d_boxes, unsig
 
 extern "C" int gb_layer_ncell(gb_layer* L) { return L ? L->ncell : 0; }
 
+extern "C" int gb_layer_digest(gb_context* ctx, gb_layer* L, unsigned long long* out) {
+  if (!ctx || !L || L->dead || !out || !L->binned) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, (size_t)L->ncell * 8) != cudaSuccess) return set_err(ctx, GB_ERR_OOM, "digest buffer");
+  cudaMemsetAsync(d, 0, (size_t)L->ncell * 8, c.stream);
+  gb_launch_digest(c, L->d, d, 1);
+  cudaStreamSynchronize(c.stream);
+  const cudaError_t ce = cudaMemcpy(out, d, (size_t)L->ncell * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (ce != cudaSuccess) return set_err(ctx, GB_ERR_CUDA, "digest copy");
+  return gb_sync(ctx, nullptr);
+}
+
 extern "C" int gb_layer_count(gb_context* ctx, gb_layer* L, long long* total, long long* per_cell) {
   if (!ctx || !L || L->dead) return GB_ERR_ARG;
   GbCtx& c = ctx->c;
@@ -559,6 +573,30 @@ extern "C" int gb_layer_to_host(gb_context* ctx, gb_layer* L, c_box* out, unsign
   if (sc[2] && out) cudaMemcpy(out, (void*)sc[0], (size_t)sc[2] * 16, cudaMemcpyDeviceToHost);
   return GB_OK;
 }
+
+namespace gbi {
+// The layer's boxes in device memory (global coordinates): a raw layer's own
+// array, or a binned layer exported into the work arena (valid until the
+// arena is released past it).
+int layer_device_boxes(gb_context* ctx, gb_layer* L, const c_box** d_boxes, long long* n) {
+  if (!ctx || !L || L->dead || !d_boxes || !n) return GB_ERR_ARG;
+  GbCtx& c = ctx->c;
+  if (!L->binned) {
+    DLayer d = read_desc(ctx, L);
+    *d_boxes = (const c_box*)d.boxes;
+    *n = d.nbox;
+    return GB_OK;
+  }
+  gb_launch_export(c, L->d, nullptr, nullptr);
+  int e = gb_sync(ctx, nullptr);
+  if (e) return e;
+  long long sc[4];
+  cudaMemcpy(sc, c.dscal, sizeof(sc), cudaMemcpyDeviceToHost);
+  *d_boxes = (const c_box*)sc[0];
+  *n = sc[2];
+  return GB_OK;
+}
+}  // namespace gbi
 
 extern "C" void gb_layer_free(gb_context* ctx, gb_layer* L) {
   if (!ctx || !L) return;

@@ -513,6 +513,37 @@ __global__ void k_export(const DLayer* L, const long long* dscal, DStatus* st) {
   }
 }
 
+// Per-cell digest of a binned layer: the sum (mod 2^64) of gb_strip_hash over
+// its strips in global coordinates.  A sum is independent of the strip order,
+// so two layers with the same canonical strips per cell have equal digests
+// whatever order their tiles were written in.  One warp per tile.
+__global__ void k_cell_digest(const DLayer* L, unsigned long long* out, int stride) {
+  const long long nt = L->ntiles;
+  const int g = L->g;
+  const int wpb = blockDim.x >> 5;
+  for (long long t = (long long)blockIdx.x * wpb + gb_warp(); t < nt; t += (long long)gridDim.x * wpb) {
+    const int cnt = L->tcount[t];
+    if (cnt == 0) continue;
+    int k, tx, ty;
+    tile_of_index(L, t, k, tx, ty);
+    const unsigned long long* p = L->pcs + L->tstart[t];
+    const int ox = tx << g, oy = ty << g;
+    unsigned long long h = 0;
+    for (int j = gb_lane(); j < cnt; j += 32) {
+      int a, b, cc, d;
+      gb_unpack(p[j], a, b, cc, d);
+      h += gb_strip_hash(ox + a, oy + b, ox + cc, oy + d);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if (gb_lane() == 0) atomicAdd(&out[(size_t)k * stride], h);
+  }
+}
+
+void gb_launch_digest(GbCtx& c, const DLayer* L, unsigned long long* out, int stride) {
+  k_cell_digest<<<c.work_blocks, 256, 0, c.stream>>>(L, out, stride);
+}
+
 void gb_launch_export(GbCtx& c, const DLayer* L, int4** out_ptr_dev, long long* total_dev) {
   (void)out_ptr_dev;
   (void)total_dev;

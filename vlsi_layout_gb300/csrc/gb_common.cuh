@@ -88,6 +88,24 @@ __host__ __device__ inline void gb_unpack(unsigned long long p, int& x1, int& y1
 }
 __host__ __device__ inline int gb_floor_shift(int v, int g) { return v >> g; }  // arithmetic shift = floor
 
+// Hash of one strip in global coordinates, for order-independent per-cell
+// digests (sum mod 2^64 over a layer's strips): the MurmurHash3 64-bit
+// finaliser (fmix64) applied to the packed corners.  The oracle computes the
+// same function.
+__host__ __device__ inline unsigned long long gb_fmix64(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return k;
+}
+__host__ __device__ inline unsigned long long gb_strip_hash(int x1, int y1, int x2, int y2) {
+  const unsigned long long u = ((unsigned long long)(unsigned)x1 << 32) | (unsigned)y1;
+  const unsigned long long v = ((unsigned long long)(unsigned)x2 << 32) | (unsigned)y2;
+  return gb_fmix64(u ^ gb_fmix64(v + 0x9e3779b97f4a7c15ull));
+}
+
 __device__ inline void gb_set_error(DStatus* st, int code, int where, long long need) {
   if (atomicCAS(&st->err, 0, code) == 0) {
     st->where = where;

@@ -151,11 +151,12 @@ extern "C" void gb_graph_destroy(gb_graph* G) {
   delete G;
 }
 
-extern "C" int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs) {
-  if (!ctx || !P || !outs || P->dead) return GB_ERR_ARG;
+// The OP1 chain (op_template.m4:14-22) on every cell of P, one scanline pass
+// per operator.  *F / *Q (optional) receive the erosion's frame and complement.
+static int op1_chain(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs, gb_layer** F, gb_layer** Q) {
   gb_layer* p1 = a >= 0 ? op_grow(ctx, P, a, a, a, a, true) : op_erode(ctx, P, -a);
-  gb_layer* p2 = a > 0 ? op_erode(ctx, P, a) : (a == 0 ? op_bool(ctx, GB_OP_MERGE, P, nullptr, 0)
-                                                        : op_grow(ctx, P, -a, -a, -a, -a, true));
+  gb_layer* p2 = a > 0 ? op_erode(ctx, P, a, F, Q)
+                       : (a == 0 ? op_bool(ctx, GB_OP_MERGE, P, nullptr, 0) : op_grow(ctx, P, -a, -a, -a, -a, true));
   if (!p1 || !p2) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
   gb_layer* outer = op_bool(ctx, GB_OP_NOT, p1, P, 0);
   gb_layer* inner = op_bool(ctx, GB_OP_NOT, P, p2, 0);
@@ -165,6 +166,11 @@ extern "C" int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs) 
   if (!and1 || !inter) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
   outs[0] = p1; outs[1] = p2; outs[2] = outer; outs[3] = inner; outs[4] = and1; outs[5] = inter;
   return GB_OK;
+}
+
+extern "C" int gb_op1(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** outs) {
+  if (!ctx || !P || !outs || P->dead) return GB_ERR_ARG;
+  return op1_chain(ctx, P, a, outs, nullptr, nullptr);
 }
 
 // Union area of P per cell from the erosion's complement: the frame F of a
@@ -191,17 +197,8 @@ extern "C" int gb_op1_area(gb_context* ctx, gb_layer* P, int32_t a, gb_layer** o
   GbCtx& c = ctx->c;
   gb_layer* F = nullptr;
   gb_layer* Q = nullptr;
-  gb_layer* p1 = a >= 0 ? op_grow(ctx, P, a, a, a, a, true) : op_erode(ctx, P, -a);
-  gb_layer* p2 = a > 0 ? op_erode(ctx, P, a, &F, &Q)
-                       : (a == 0 ? op_bool(ctx, GB_OP_MERGE, P, nullptr, 0) : op_grow(ctx, P, -a, -a, -a, -a, true));
-  if (!p1 || !p2) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
-  gb_layer* outer = op_bool(ctx, GB_OP_NOT, p1, P, 0);
-  gb_layer* inner = op_bool(ctx, GB_OP_NOT, P, p2, 0);
-  if (!outer || !inner) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
-  gb_layer* and1 = op_bool(ctx, GB_OP_AND, outer, P, 0);
-  gb_layer* inter = op_bool(ctx, GB_OP_AND, outer, inner, 0);
-  if (!and1 || !inter) return set_err(ctx, GB_ERR_CAPACITY, "descriptor pool exhausted");
-  outs[0] = p1; outs[1] = p2; outs[2] = outer; outs[3] = inner; outs[4] = and1; outs[5] = inter;
+  const int e = op1_chain(ctx, P, a, outs, &F, &Q);
+  if (e) return e;
   const int nb = (P->ncell + 255) / 256;
   if (F && Q) {
     k_area_from_frame<<<nb, 256, 0, c.stream>>>(F->d, Q->d, d_area, P->ncell, c.st);
@@ -228,9 +225,9 @@ __global__ void k_gather_counts(const DLayer* const* L, int nl, int ncell, long 
 // split at a cell boundary when the layer is large; each half's deck starts
 // when its copy has landed, so the second copy overlaps the first half's
 // work.  Counts and areas come back with one copy each at the end.
-extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
-                           const long long* cell_offsets, int ncell, int32_t a, long long* counts,
-                           long long* area, int* assert_failures) {
+static int op1_host_impl(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                         const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                         long long* area, unsigned long long* digests, int* assert_failures) {
   if (!ctx || (!boxes && n) || ncell < 1) return GB_ERR_ARG;
   if (!cell_offsets) ncell = 1;
   GbCtx& c = ctx->c;
@@ -278,10 +275,12 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
   }
   long long* dcounts = nullptr;
   long long* darea = nullptr;
+  unsigned long long* ddig = nullptr;
   DLayer** dl = nullptr;
   int e = GB_OK;
   if (cudaMalloc(&dcounts, (size_t)ncell * 6 * 8) != cudaSuccess || cudaMalloc(&darea, (size_t)ncell * 8) != cudaSuccess ||
-      cudaMalloc(&dl, 8 * sizeof(DLayer*)) != cudaSuccess)
+      cudaMalloc(&dl, 8 * sizeof(DLayer*)) != cudaSuccess ||
+      (digests && cudaMalloc(&ddig, (size_t)ncell * 6 * 8) != cudaSuccess))
     e = set_err(ctx, GB_ERR_OOM, "deck result buffers");
   for (int g = 0; g < ng && !e; ++g) {
     const int k0 = cut[g], k1 = cut[g + 1];
@@ -302,6 +301,10 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
       cudaMemcpyAsync(dl, hl, sizeof(hl), cudaMemcpyHostToDevice, c.stream);
       k_gather_counts<<<(gn + 255) / 256, 256, 0, c.stream>>>(dl, 6, gn, dcounts + (size_t)k0 * 6, nullptr, nullptr,
                                                              c.st);
+      if (ddig) {  // per-cell strip digests of the six layers, [cell][layer]
+        cudaMemsetAsync(ddig + (size_t)k0 * 6, 0, (size_t)gn * 6 * 8, c.stream);
+        for (int j = 0; j < 6; ++j) gb_launch_digest(c, outs[j]->d, ddig + (size_t)k0 * 6 + j, 6);
+      }
       return GB_OK;
     });
     gb_layer_free(ctx, P);
@@ -316,13 +319,28 @@ extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long lo
     if (assert_failures) *assert_failures = fails;
     if (counts) memcpy(counts, hc.data(), hc.size() * 8);
     if (area) memcpy(area, ha.data(), ha.size() * 8);
+    if (digests) cudaMemcpy(digests, ddig, (size_t)ncell * 6 * 8, cudaMemcpyDeviceToHost);
   }
   for (cudaEvent_t x : ev) cudaEventDestroy(x);
   cudaEventDestroy(ready);
   if (dcounts) cudaFree(dcounts);
   if (darea) cudaFree(darea);
+  if (ddig) cudaFree(ddig);
   if (dl) cudaFree(dl);
   return e;
+}
+
+extern "C" int gb_op1_host(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                           const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                           long long* area, int* assert_failures) {
+  return op1_host_impl(ctx, boxes, n, cell_offsets, ncell, a, counts, area, nullptr, assert_failures);
+}
+
+extern "C" int gb_op1_host_digest(gb_context* ctx, const c_box* boxes, unsigned long long n,
+                                  const long long* cell_offsets, int ncell, int32_t a, long long* counts,
+                                  long long* area, unsigned long long* digests, int* assert_failures) {
+  if (!digests) return GB_ERR_ARG;
+  return op1_host_impl(ctx, boxes, n, cell_offsets, ncell, a, counts, area, digests, assert_failures);
 }
 
 // Slab height of the operators: the OP1 chain with the union area runs on P

@@ -9,6 +9,8 @@
 #include <mutex>
 #include "gb_common.cuh"
 
+struct c_box;  // include/gbool.h
+
 #define GB_SCAN_BLOCKS 256
 #define GB_SCAN_THREADS 512
 #define GB_TILE_THREADS 384
@@ -86,6 +88,9 @@ DLayer read_desc(gb_context* ctx, gb_layer* L);
 // keeps them alive while the layer is used), cells given by host offsets.
 int layer_over_device(gb_context* ctx, const void* d_boxes, long long n, const long long* h_offsets, int ncell,
                       gb_layer** out);
+// The layer's boxes in device memory: a raw layer's array, or a binned layer
+// exported into the work arena.
+int layer_device_boxes(gb_context* ctx, gb_layer* L, const c_box** d_boxes, long long* n);
 }
 gb_layer* op_bool(gb_context* ctx, int op, gb_layer* A, gb_layer* B, int mode);
 gb_layer* op_grow(gb_context* ctx, gb_layer* A, int E, int N, int W, int S, bool merge);
@@ -121,6 +126,9 @@ void gb_launch_bool_setup(GbCtx& c, int op, const DLayer* A, const DLayer* B, DL
 // device pointer to the box array and the total land in *dscal-slots.
 void gb_launch_export(GbCtx& c, const DLayer* L, int4** out_ptr_dev, long long* total_dev);
 void gb_launch_cell_bbox_fill(GbCtx& c, DLayer* L, int ncell);
+// Per-cell strip digests of a binned layer, added to out[cell * stride]
+// (out zeroed by the caller).
+void gb_launch_digest(GbCtx& c, const DLayer* L, unsigned long long* out, int stride);
 
 // ---- tile kernel (gb_tile.cu)
 void gb_tile_setup(GbCtx& c);

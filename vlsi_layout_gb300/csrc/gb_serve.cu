@@ -110,9 +110,16 @@ extern "C" int gb_serve_add_layer(gb_server* S, const c_box* boxes, unsigned lon
   if (e) return e;
   // bin once; the binned form lives in the home context's arena for the server's lifetime
   gb_layer* B = binned_of(S->home, L, 16);
-  if (!B) return GB_ERR_CAPACITY;
+  if (!B) {
+    gb_layer_free(S->home, L);  // not recorded: gb_serve_destroy would never free it
+    return GB_ERR_CAPACITY;
+  }
   e = gb_sync(S->home, nullptr);
-  if (e) return e;
+  if (e) {
+    gb_layer_free(S->home, B);
+    gb_layer_free(S->home, L);
+    return e;
+  }
   *id = (int)S->raw.size();
   S->raw.push_back(L);
   S->binned.push_back(B);

@@ -341,7 +341,25 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     atomicAdd((unsigned long long*)&tctr[8], (unsigned long long)qsetup);
     atomicAdd((unsigned long long*)&tctr[9], (unsigned long long)qpaint);
   }
-  for (int c = c0; c < c1e; ++c) ca[c] = gb_pred(op, ca[c], cb[c]);
+  unsigned long long rany = 0;
+  for (int c = c0; c < c1e; ++c) {
+    const unsigned long long r = gb_pred(op, ca[c], cb[c]);
+    ca[c] = r;
+    rany |= r;
+  }
+  // No region in rows 1..63: the sub-band has no strip pieces (row 0 belongs to
+  // the previous sub-band, and its runs matter only to continuations here).
+  if (!__any_sync(0xffffffffu, (rany & ~1ull) != 0ull)) {
+    if (lane == 0) {
+      s.sbinfo[sb] = make_int4(0, 0, 0, 0);
+      s.sbh[sb] = 0;
+      s.sbct[sb] = 0;
+      s.sbol[sb] = nullptr;
+      s.sbrec[sb] = nullptr;
+    }
+    __syncwarp();
+    return;
+  }
   __syncwarp();
   TSTEP(1)
   // ---- run starts S_c = R_c & ~R_{c-1}, transposed to one column bitmap per row

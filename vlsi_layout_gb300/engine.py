@@ -86,6 +86,8 @@ def lib():
         "device_event_sort": (None, [P, i64]),
         "gb_op1": (ctypes.c_int, [P, P, i32, P]),
         "gb_op1_host": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P]),
+        "gb_op1_host_digest": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P, P]),
+        "gb_layer_digest": (ctypes.c_int, [P, P, P]),
         "gb_op1_area": (ctypes.c_int, [P, P, i32, P, P]),
         "gb_graph_begin": (ctypes.c_int, [P]),
         "gb_graph_end": (ctypes.c_int, [P, pp]),
@@ -147,6 +149,13 @@ class Layer:
         per = np.zeros(self.ncell, np.int64)
         self.ctx._chk(lib().gb_layer_count(self.ctx.h, self.h, ctypes.byref(t), per.ctypes.data))
         return int(t.value), per
+
+    def digest(self):
+        """Per-cell digest of the layer's strips (uint64, order-independent;
+        gb_layer_digest)."""
+        out = np.zeros(self.ncell, np.uint64)
+        self.ctx._chk(lib().gb_layer_digest(self.ctx.h, self.h, out.ctypes.data))
+        return out
 
     def to_numpy(self, with_cells=False):
         n = ctypes.c_uint64()
@@ -281,15 +290,22 @@ class Context:
         self._chk(lib().gb_op1_area(self.h, P.h, amount, outs, area_ptr))
         return [Layer(self, ctypes.c_void_p(outs[i]), P.ncell) for i in range(6)]
 
-    def op1_host(self, boxes_ptr, n, offsets, amount):
+    def op1_host(self, boxes_ptr, n, offsets, amount, digests=False):
         """OP1 deck through host buffers (boxes_ptr: address of n int32x4
         boxes, e.g. pinned memory).  Returns (counts[ncell,6], area[ncell],
-        assert_failures)."""
+        assert_failures), plus digests[ncell,6] (uint64 per cell and result
+        layer) when digests is true."""
         off = np.ascontiguousarray(offsets, np.int64)
         ncell = len(off) - 1
         counts = np.zeros((ncell, 6), np.int64)
         area = np.zeros(ncell, np.int64)
         fails = ctypes.c_int()
+        if digests:
+            dig = np.zeros((ncell, 6), np.uint64)
+            self._chk(lib().gb_op1_host_digest(self.h, ctypes.c_void_p(boxes_ptr), n, off.ctypes.data, ncell, amount,
+                                               counts.ctypes.data, area.ctypes.data, dig.ctypes.data,
+                                               ctypes.byref(fails)))
+            return counts, area, fails.value, dig
         self._chk(lib().gb_op1_host(self.h, ctypes.c_void_p(boxes_ptr), n, off.ctypes.data, ncell, amount,
                                     counts.ctypes.data, area.ctypes.data, ctypes.byref(fails)))
         return counts, area, fails.value
