@@ -122,6 +122,7 @@ def ncu_traffic():
     return None
 
 
+ARENA_BYTES = 0  # device work arena of every context the bench opens (0: the engine's default); --arena-gb
 CPU_SAMPLE_BOXES = 4_000_000  # the CPU legs' sample: the first cells holding about this many boxes
 
 
@@ -249,7 +250,7 @@ def sort_leg(n=200_000_000, steps=5, seed=5, tune=True):
     torch.cuda.set_stream(stream)
     peak, kind = peaks()
     out = {"n": n, "peak": peak}
-    with engine.Context(0) as ctx:
+    with engine.Context(0, ARENA_BYTES) as ctx:
         ctx.set_stream(stream.cuda_stream)
         k0 = torch.empty_like(keys)
         v0 = torch.empty_like(vals)
@@ -386,7 +387,7 @@ def snap_leg(n_per=10_000_000, steps=3, cpu_chunks=96):
     torch.cuda.set_stream(stream)
     res = {"n": n, "method": "snappy", "workload": "stdcell layers (poly, met1, met2, li1 x %d + 2%% contacts, "
            "4e7 die), Morton sorted" % n_per}
-    with engine.Context(0) as ctx:
+    with engine.Context(0, ARENA_BYTES) as ctx:
         ctx.set_stream(stream.cuda_stream)
         d = torch.from_numpy(B).cuda()
         keys = torch.empty(n, dtype=torch.int64, device="cuda")
@@ -469,7 +470,7 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
     n = len(B)
     res = {"n": n, "workload": "stdcell layers (poly, met1, met2, li1 x %d + 2%% contacts, die %d dbu) as one "
            "layer" % (n_per, int(400_000 * (n_per / 100_000) ** 0.5))}
-    with engine.Context(0) as ctx:
+    with engine.Context(0, ARENA_BYTES) as ctx:
         # Klee's-measure area of the layout (one cell): binning + count-mode union on the device
         L = ctx.layer(B)
         ctx.sync()
@@ -514,7 +515,7 @@ def connectivity_leg(n_per=5_000_000, steps=3, cpu_scale=10):
     t2 = time.perf_counter()
     ea = O.union_area(S)
     t3 = time.perf_counter()
-    with engine.Context(0) as ctx:  # parity on the sample: labels, pair count, singleton mask, area
+    with engine.Context(0, ARENA_BYTES) as ctx:  # parity on the sample: labels, pair count, singleton mask, area
         gn, glab = ctx.components(S)
         gp, gs, gmask = ctx.interactions(S)
         LS = ctx.layer(S)
@@ -610,7 +611,12 @@ def main():
     ap.add_argument("--no-conn", action="store_true")
     ap.add_argument("--no-snap", action="store_true")
     ap.add_argument("--snap-n", type=int, default=10_000_000, help="boxes per stdcell layer of the SNAP leg")
+    ap.add_argument("--arena-gb", type=float, default=0.0,
+                    help="device work arena per context in GB (0: the engine's default, up to 120 GB); a small one "
+                         "keeps profiler captures small")
     args = ap.parse_args()
+    global ARENA_BYTES
+    ARENA_BYTES = int(args.arena_gb * (1 << 30))
     world, rank, local, dist = dist_init()
     if args.sort_only:
         import torch
@@ -649,7 +655,7 @@ def main():
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream()  # a real stream: the engine launches and the events record on it
     torch.cuda.set_stream(stream)
-    ctx = engine.Context(local)
+    ctx = engine.Context(local, ARENA_BYTES)
     ctx.set_stream(stream.cuda_stream)
     P = ctx.layer(boxes, off)
     ctx.sync()

@@ -799,16 +799,31 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     }
     __syncthreads();
     if (timing) { const long long t1 = clock64(); tB += t1 - t0; t0 = t1; }
-    // ---- C: one warp per sub-band, handed out dynamically
+    // ---- C: one warp per sub-band, handed out dynamically, the ones with the most members first
+    // (longest processing time first: the phase ends with the last sub-band, so the large ones must
+    // not come last).  The order lives in the value-table region, unused until phase D.
+    int* const ord = s.xyv + TK_MD_INTS;
+    const bool lpt = !s.err && nsb > TK_NW && nsb <= TK_SBS;
+    if (lpt) {
+      for (int q = tid; q < nsb; q += TK_NT) {
+        const int mq = s.sbc[q] - (q ? s.sbc[q - 1] : 0);
+        int r = 0;
+        for (int j = 0; j < nsb; ++j) {
+          const int mj = s.sbc[j] - (j ? s.sbc[j - 1] : 0);
+          r += (mj > mq) || (mj == mq && j < q);
+        }
+        ord[r] = q;
+      }
+    }
     if (tid == 0) s.sbnext = 0;
     __syncthreads();
     if (!s.err) {
       for (;;) {
-        int sb = 0;
-        if (gb_lane() == 0) sb = atomicAdd(&s.sbnext, 1);
-        sb = __shfl_sync(0xffffffffu, sb, 0);
-        if (sb >= nsb) break;
-        tile_subband(s, op, sb, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
+        int k = 0;
+        if (gb_lane() == 0) k = atomicAdd(&s.sbnext, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= nsb) break;
+        tile_subband(s, op, lpt ? ord[k] : k, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
       }
     }
     // the bulk copies of phase D (async proxy) read the records written above and overwrite shared
@@ -918,20 +933,37 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     const long long obase = s.obase;
     unsigned long long* outp = obase >= 0 ? O->pcs + obase : nullptr;
     long long area = 0;
-    for (int sb = wid; sb < nsb; sb += TK_NW) {
-      const int4 inf = s.sbinfo[sb];
-      for (int j = lane; j < inf.y; j += 32) {
-        const int p = inf.x + j;
-        const PieceRec pr = REC(sb, p);
+    if (prs) {
+      // records on chip: every thread takes pieces in turn; a piece's sub-band is its first slab / 63
+      // (its first row is 1..63 of that sub-band)
+      for (int p = tid; p < NP; p += TK_NT) {
+        const PieceRec pr = PR[p];
         if (pr_cont(pr)) continue;
-        int q = p, sq = sb, guard = 0;
-        while (succ[q] >= 0 && guard++ <= nsb) { q = succ[q]; ++sq; }
-        const int shi = q == p ? pr_shi(pr) : pr_shi(REC(sq, q));
+        int q = p, guard = 0;
+        while (succ[q] >= 0 && guard++ <= nsb) q = succ[q];
+        const int shi = q == p ? pr_shi(pr) : pr_shi(PR[q]);
         const int slo = pr_slo(pr);
         const int xs = Xv[slo], xe = Xv[shi], ylo = Yv[pr_ylo(pr)], yhi = Yv[pr_yhi(pr)];
-        const int pos = s.sbh[sb] + pr_hrank(pr);
+        const int pos = s.sbh[slo / 63] + pr_hrank(pr);
         if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
         area += (long long)(xe - xs) * (long long)(yhi - ylo);
+      }
+    } else {
+      for (int sb = wid; sb < nsb; sb += TK_NW) {
+        const int4 inf = s.sbinfo[sb];
+        for (int j = lane; j < inf.y; j += 32) {
+          const int p = inf.x + j;
+          const PieceRec pr = REC(sb, p);
+          if (pr_cont(pr)) continue;
+          int q = p, sq = sb, guard = 0;
+          while (succ[q] >= 0 && guard++ <= nsb) { q = succ[q]; ++sq; }
+          const int shi = q == p ? pr_shi(pr) : pr_shi(REC(sq, q));
+          const int slo = pr_slo(pr);
+          const int xs = Xv[slo], xe = Xv[shi], ylo = Yv[pr_ylo(pr)], yhi = Yv[pr_yhi(pr)];
+          const int pos = s.sbh[sb] + pr_hrank(pr);
+          if (outp) outp[pos] = gb_pack(xs, ylo, xe, yhi);
+          area += (long long)(xe - xs) * (long long)(yhi - ylo);
+        }
       }
     }
     area = gb_block_sum(area, s.tmp64);
