@@ -130,6 +130,57 @@ __device__ __forceinline__ void warp_bbox_atomic(int4* dst, int x1, int y1, int 
   }
 }
 
+// Raw-source kernels walk the boxes in one contiguous chunk per warp (the
+// boxes divided evenly over the grid's warps, in multiples of 32), 32
+// consecutive boxes per step (coalesced), BIN_LD steps loaded before any is
+// processed.  The cell of a box comes from one search of the cell
+// offsets at the chunk's start; after that a lane only steps past the cells
+// that end before its box (cells are sorted and hold many boxes, so nearly
+// always none), which removes the dependent chain of a binary search per box.
+#define BIN_LD 4
+
+template <int LD, typename F>
+__device__ __forceinline__ void walk_raw_boxes(const int4* bx, const long long* coff, int ncell, long long n, F f) {
+  const int lane = gb_lane();
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long ch = max(32ll, (((n + nw - 1) / nw) + 31) & ~31ll);
+  for (long long c0 = ((long long)blockIdx.x * (blockDim.x >> 5) + gb_warp()) * ch; c0 < n; c0 += nw * ch) {
+    const long long c1 = min(n, c0 + ch);
+    int k = 0;
+    long long hi = 0;
+    if (lane == 0) {
+      k = gb_find_cell(coff, ncell, c0);
+      hi = coff[k + 1];
+    }
+    k = __shfl_sync(0xffffffffu, k, 0);
+    hi = __shfl_sync(0xffffffffu, hi, 0);
+    for (long long b0 = c0; b0 < c1; b0 += 32 * LD) {
+      int4 ld[LD];
+#pragma unroll
+      for (int u = 0; u < LD; ++u) {
+        const long long i = b0 + 32 * u + lane;
+        if (i < c1) ld[u] = bx[i];
+      }
+#pragma unroll
+      for (int u = 0; u < LD; ++u) {
+        const long long b = b0 + 32 * u;
+        if (b >= c1) break;  // warp-uniform
+        const long long i = b + lane;
+        int kl = k;
+        long long hl = hi;
+        if (i < c1)
+          while (i >= hl && kl + 1 < ncell) {
+            ++kl;
+            hl = coff[kl + 1];
+          }
+        f(i, i < c1, ld[u], kl);  // called by all lanes (warp collectives allowed)
+        k = __shfl_sync(0xffffffffu, kl, 31);  // the last lane holds the furthest cell
+        hi = __shfl_sync(0xffffffffu, hl, 31);
+      }
+    }
+  }
+}
+
 // Raw source: one thread per box; boxes of a warp can straddle cells, so the
 // warp reduces per cell only when all lanes agree, else atomics per lane.
 __global__ void k_bbox_raw(const DLayer* S, DLayer* O, int ncell, int E, int N, int W, int Sg,
@@ -138,17 +189,15 @@ __global__ void k_bbox_raw(const DLayer* S, DLayer* O, int ncell, int E, int N, 
   const long long n = S->nbox;
   const int4* bx = S->boxes;
   const long long* coff = S->coff;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
-    const long long i = base + threadIdx.x;
+  walk_raw_boxes<BIN_LD>(bx, coff, ncell, n, [&](long long i, bool valid_i, int4 box, int kc) {
     int x1 = INT32_MAX, y1 = INT32_MAX, x2 = INT32_MIN, y2 = INT32_MIN, k = -1;
-    if (i < n) {
+    if (valid_i) {
       int4 g;
-      if (!grow_box(bx[i], E, N, W, Sg, g)) {
+      if (!grow_box(box, E, N, W, Sg, g)) {
         gb_set_error(st, GB_ERR_INVALID_BOX, KID_BBOX, i);
       } else {
         x1 = g.x; y1 = g.y; x2 = g.z; y2 = g.w;
-        k = gb_find_cell(coff, ncell, i);
+        k = kc;
       }
     }
     const int k0 = __shfl_sync(0xffffffffu, k, 0);
@@ -168,7 +217,7 @@ __global__ void k_bbox_raw(const DLayer* S, DLayer* O, int ncell, int E, int N, 
       atomicMax(&O->cbox[k].z, x2);
       atomicMax(&O->cbox[k].w, y2);
     }
-  }
+  });
 }
 
 __device__ __forceinline__ void tile_of_index(const DLayer* L, long long t, int& k, int& tx, int& ty) {
@@ -307,14 +356,12 @@ template <int MODE, bool SCATTER>
 __global__ void k_split_raw(const DLayer* S, DLayer* O, int ncell, int g, int E, int N, int W,
                             int Sg, DStatus* st) {
   if (st->err) return;
-  const long long n = S->nbox;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+  walk_raw_boxes<SCATTER ? 2 : BIN_LD>(S->boxes, S->coff, ncell, S->nbox,
+                                       [&](long long i, bool valid_i, int4 box, int k) {
     int4 b;
-    if (!grow_box(S->boxes[i], E, N, W, Sg, b)) continue;  // already reported by k_bbox_raw
-    const int k = gb_find_cell(S->coff, ncell, i);
+    if (!valid_i || !grow_box(box, E, N, W, Sg, b)) return;  // invalid: reported by k_bbox_raw
     emit_box_tiles<MODE, SCATTER>(O, k, b, i, g);
-  }
+  });
 }
 
 template <bool SCATTER>

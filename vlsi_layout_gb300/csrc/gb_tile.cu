@@ -91,6 +91,7 @@ struct TileSmem {
       unsigned srow[TK_NW][64][TK_LCN / 32];  // run starts, row-major (transposed)
     };
     unsigned char dbuf[1];
+    int4 dbuf_align;  // the region starts on 16 bytes: bulk copies and int4 records land in it
   };
   int sbnext;                            // next sub-band to hand to a warp
   unsigned long long mbar;               // completion of phase D's bulk copies (one phase per tile)
@@ -115,6 +116,14 @@ struct TileSmem {
   unsigned* biglb;
   int* succ;
 };
+#include <cstddef>
+// Bulk asynchronous copies need 16-byte aligned shared-memory addresses, and
+// the staged ranks, piece records and sub-band metadata are read as int4.
+static_assert(offsetof(TileSmem, dbuf) % 16 == 0, "phase C/D region must start on 16 bytes");
+static_assert(offsetof(TileSmem, xyv) % 16 == 0, "value-table region must start on 16 bytes");
+static_assert(offsetof(TileSmem, ca) % 16 == 0 && offsetof(TileSmem, srow) % 16 == 0, "per-warp arrays");
+static_assert((TK_MD_INTS * 4) % 16 == 0, "value tables after the metadata start on 16 bytes");
+
 
 __device__ __forceinline__ unsigned long long gb_pred(int op, unsigned long long a, unsigned long long b) {
   switch (op) {

@@ -9,13 +9,18 @@
 //
 // Candidate pairs come from a closed-range tile binning (every box is listed
 // in each tile its closed extent touches, so two touching boxes share at
-// least one tile).  One CTA per tile tests all pairs of its boxes and hooks
-// roots with atomicCAS, the larger root under the smaller, so the surviving
-// root is the component minimum.  Pointer jumping then flattens the forest.
+// least one tile).  Tiles of up to UF_WARP_BOXES boxes (nearly all: the grid
+// is sized for about 32 boxes per tile) are taken one per warp, with the
+// tile's boxes staged in the warp's shared memory; larger tiles are taken one
+// per CTA.  Every pair that meets is hooked with atomicCAS, the larger root
+// under the smaller, so the surviving root is the component minimum whatever
+// the order of the hooks.  Pointer jumping then flattens the forest.
 #include "gb_internal.h"
 #include "gb_scan.cuh"
 
 #define UF_SMEM_BOXES 1024
+#define UF_WARP_BOXES 64   // tiles up to this size go one per warp
+#define UF_WARPS 8         // warps per CTA of the per-warp kernels
 #define KID_UF 30
 
 __device__ __forceinline__ int uf_find(int* parent, int x) {
@@ -55,24 +60,66 @@ __device__ __forceinline__ bool closed_overlap(int4 a, int4 b) {
   return max(a.x, b.x) <= min(a.z, b.z) && max(a.y, b.y) <= min(a.w, b.w);
 }
 
-__global__ void __launch_bounds__(256) k_uf_tile(const DLayer* raw, const DLayer* bin, int* parent,
-                                                 unsigned char* touched, long long* counter,
-                                                 DStatus* st) {
-  __shared__ int4 sb[UF_SMEM_BOXES];
-  __shared__ int si[UF_SMEM_BOXES];
-  __shared__ long long s_t;
+// The tile's pairs, one warp per tile of at most UF_WARP_BOXES boxes (tiles
+// are taken in a grid stride over all warps; larger tiles are skipped and left
+// to the per-CTA kernel).  act(ia, ba, ib, bb, t) handles one pair that meets.
+template <typename Act>
+__device__ __forceinline__ void warp_tiles(const DLayer* raw, const DLayer* bin, int4 (*sb)[UF_WARP_BOXES],
+                                           int (*si)[UF_WARP_BOXES], Act act) {
   const int4* boxes = raw->boxes;
   const int* idx = (const int*)bin->pcs;
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_t = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
-    __syncthreads();
-    const long long t = s_t;
-    if (t >= bin->ntiles) break;
+  const int w = gb_warp(), lane = gb_lane();
+  const long long nt = bin->ntiles;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long t = (long long)blockIdx.x * (blockDim.x >> 5) + w; t < nt; t += nwarps) {
     const int k = bin->tcount[t];
-    if (k < 2) continue;
+    if (k < 2 || k > UF_WARP_BOXES) continue;
+    const int* ti = idx + bin->tstart[t];
+    for (int j = lane; j < k; j += 32) {
+      const int i = ti[j];
+      si[w][j] = i;
+      sb[w][j] = boxes[i];
+    }
+    __syncwarp();
+    for (int a = 0; a + 1 < k; ++a) {
+      const int ia = si[w][a];
+      const int4 ba = sb[w][a];
+      for (int b = a + 1 + lane; b < k; b += 32) {
+        const int4 bb = sb[w][b];
+        if (closed_overlap(ba, bb)) act(ia, ba, si[w][b], bb, t);
+      }
+    }
+    __syncwarp();  // the next tile overwrites the warp's boxes
+  }
+}
+
+__global__ void __launch_bounds__(UF_WARPS * 32) k_uf_tile_warp(const DLayer* raw, const DLayer* bin, int* parent,
+                                                              unsigned char* touched, DStatus* st) {
+  __shared__ int4 sb[UF_WARPS][UF_WARP_BOXES];
+  __shared__ int si[UF_WARPS][UF_WARP_BOXES];
+  if (st->err) return;
+  warp_tiles(raw, bin, sb, si, [&](int ia, int4, int ib, int4, long long) {
+    touched[ia] = 1;
+    touched[ib] = 1;
+    uf_unite(parent, ia, ib, st);
+  });
+}
+
+// Tiles of more than UF_WARP_BOXES boxes, one per CTA (a grid stride over
+// the tiles; the others are skipped without a barrier).
+__global__ void __launch_bounds__(256) k_uf_tile(const DLayer* raw, const DLayer* bin, int* parent,
+                                                 unsigned char* touched, DStatus* st) {
+  __shared__ int4 sb[UF_SMEM_BOXES];
+  __shared__ int si[UF_SMEM_BOXES];
+  const int4* boxes = raw->boxes;
+  const int* idx = (const int*)bin->pcs;
+  if (st->err) return;
+  for (long long t = blockIdx.x; t < bin->ntiles; t += gridDim.x) {
+    const int k = bin->tcount[t];
+    if (k <= UF_WARP_BOXES) continue;
     const int* ti = idx + bin->tstart[t];
     const bool in_smem = k <= UF_SMEM_BOXES;
+    __syncthreads();  // the previous tile's boxes are no longer read
     if (in_smem) {
       for (int j = threadIdx.x; j < k; j += blockDim.x) { si[j] = ti[j]; sb[j] = boxes[si[j]]; }
       __syncthreads();
@@ -103,33 +150,53 @@ __device__ __forceinline__ bool strict_overlap(int4 a, int4 b) {
   return max(a.x, b.x) < min(a.z, b.z) && max(a.y, b.y) < min(a.w, b.w);
 }
 
+// A strict pair is counted in the tile holding the lower-left corner of its
+// intersection.
+__device__ __forceinline__ bool counted_here(int4 ba, int4 bb, int g, const DLayer* bin, long long t) {
+  if (!strict_overlap(ba, bb)) return false;
+  const int4 w = bin->win[0];
+  const long long li = t - bin->tbase[0];
+  const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+  return (max(ba.x, bb.x) >> g) == tx && (max(ba.y, bb.y) >> g) == ty;
+}
+
+__global__ void __launch_bounds__(UF_WARPS * 32) k_pair_stats_warp(const DLayer* raw, const DLayer* bin, int g,
+                                                                 unsigned char* touched,
+                                                                 unsigned long long* strict, DStatus* st) {
+  __shared__ int4 sb[UF_WARPS][UF_WARP_BOXES];
+  __shared__ int si[UF_WARPS][UF_WARP_BOXES];
+  if (st->err) return;
+  unsigned long long cnt = 0;
+  warp_tiles(raw, bin, sb, si, [&](int ia, int4 ba, int ib, int4 bb, long long t) {
+    touched[ia] = 1;
+    touched[ib] = 1;
+    if (counted_here(ba, bb, g, bin, t)) ++cnt;
+  });
+  cnt = gb_warp_sum(cnt);
+  if (gb_lane() == 0 && cnt) atomicAdd(strict, cnt);
+}
+
+// Tiles of more than UF_WARP_BOXES boxes, one per CTA.
 __global__ void __launch_bounds__(256) k_pair_stats(const DLayer* raw, const DLayer* bin, int g,
                                                     unsigned char* touched, unsigned long long* strict,
-                                                    long long* counter, DStatus* st) {
+                                                    DStatus* st) {
   __shared__ int4 sb[UF_SMEM_BOXES];
   __shared__ int si[UF_SMEM_BOXES];
-  __shared__ long long s_t;
   const int4* boxes = raw->boxes;
   const int* idx = (const int*)bin->pcs;
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_t = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
-    __syncthreads();
-    const long long t = s_t;
-    if (t >= bin->ntiles) break;
+  if (st->err) return;
+  unsigned long long cnt = 0;
+  for (long long t = blockIdx.x; t < bin->ntiles; t += gridDim.x) {
     const int k = bin->tcount[t];
-    if (k < 2) continue;
-    const int4 w = bin->win[0];
-    const long long li = t - bin->tbase[0];
-    const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+    if (k <= UF_WARP_BOXES) continue;
     const int* ti = idx + bin->tstart[t];
     const bool in_smem = k <= UF_SMEM_BOXES;
+    __syncthreads();  // the previous tile's boxes are no longer read
     if (in_smem) {
       for (int j = threadIdx.x; j < k; j += blockDim.x) { si[j] = ti[j]; sb[j] = boxes[si[j]]; }
       __syncthreads();
     }
     const int nw = blockDim.x >> 5;
-    unsigned long long cnt = 0;
     for (int a = gb_warp(); a < k; a += nw) {
       const int ia = in_smem ? si[a] : ti[a];
       const int4 ba = in_smem ? sb[a] : boxes[ia];
@@ -139,13 +206,13 @@ __global__ void __launch_bounds__(256) k_pair_stats(const DLayer* raw, const DLa
         if (closed_overlap(ba, bb)) {
           touched[ia] = 1;
           touched[ib] = 1;
-          if (strict_overlap(ba, bb) && (max(ba.x, bb.x) >> g) == tx && (max(ba.y, bb.y) >> g) == ty) ++cnt;
+          if (counted_here(ba, bb, g, bin, t)) ++cnt;
         }
       }
     }
-    cnt = gb_warp_sum(cnt);
-    if (gb_lane() == 0 && cnt) atomicAdd(strict, cnt);
   }
+  cnt = gb_warp_sum(cnt);
+  if (gb_lane() == 0 && cnt) atomicAdd(strict, cnt);
 }
 
 __global__ void k_singletons(const unsigned char* touched, long long n, unsigned char* mask,
@@ -200,8 +267,8 @@ void gb_launch_pair_stats(GbCtx& c, const DLayer* raw, DLayer* binidx, int g, un
   cudaMemsetAsync(touched, 0, (size_t)n, c.stream);
   cudaMemsetAsync(strict_dev, 0, 8, c.stream);
   cudaMemsetAsync(single_dev, 0, 8, c.stream);
-  k_zero_ll<<<1, 32, 0, c.stream>>>(c.tile_counter + 1, 1);
-  k_pair_stats<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, g, touched, strict_dev, c.tile_counter + 1, c.st);
+  k_pair_stats_warp<<<c.nsm * 8, UF_WARPS * 32, 0, c.stream>>>(raw, binidx, g, touched, strict_dev, c.st);
+  k_pair_stats<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, g, touched, strict_dev, c.st);
   k_singletons<<<c.work_blocks, 256, 0, c.stream>>>(touched, n, mask_dev, single_dev);
   c.launches += 3;
 }
@@ -213,8 +280,8 @@ void gb_launch_components(GbCtx& c, const DLayer* raw, DLayer* binidx, int* pare
   long long* sl = c.dscal;  // [4] nsingle, [5] nroots, [8..10] scan pointer slots
   k_zero_ll<<<1, 32, 0, c.stream>>>(sl + 4, 2);
   k_uf_init<<<wb, 256, 0, c.stream>>>(parent, touched, n);
-  k_zero_ll<<<1, 32, 0, c.stream>>>(c.tile_counter + 1, 1);
-  k_uf_tile<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, parent, touched, c.tile_counter + 1, c.st);
+  k_uf_tile_warp<<<c.nsm * 8, UF_WARPS * 32, 0, c.stream>>>(raw, binidx, parent, touched, c.st);
+  k_uf_tile<<<c.nsm * 4, 256, 0, c.stream>>>(raw, binidx, parent, touched, c.st);
   k_uf_flatten<<<wb, 256, 0, c.stream>>>(parent, touched, flag_tmp, n, sl + 4);
   k_set_ptrs<<<1, 1, 0, c.stream>>>(sl, flag_tmp, map_tmp, n);
   gb_launch_scan_i32(c, (int* const*)&sl[8], (long long* const*)&sl[9], &sl[10], sl + 5);
