@@ -201,8 +201,12 @@ __device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long lo
 }
 
 
+// TIMING: the phase counters of gb_tile_timing are compiled in (tctr non-null
+// then); the production instance has none of that code.
+template <bool TIMING>
 __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int nA, char* base,
                              unsigned long long scr, long long* tctr) {
+  if (!TIMING) tctr = nullptr;
   const int lane = gb_lane(), wid = gb_warp();
   long long q0 = tctr ? clock64() : 0;
 #define TSTEP(k) if (tctr && lane == 0) { const long long q1 = clock64(); atomicAdd((unsigned long long*)&tctr[k], (unsigned long long)(q1 - q0)); q0 = q1; }
@@ -542,6 +546,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
 #undef TSTEP
 }
 
+template <bool TIMING>
 __global__ void __launch_bounds__(TK_NT, 3)
 k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, char* scratch,
        unsigned long long scr, long long* counter, DStatus* st) {
@@ -551,7 +556,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
   char* base = scratch + (size_t)blockIdx.x * scr;
   const unsigned long long half = scr >> 1;
   const int W = ((1 << g) >> 5) + 1;
-  const bool timing = (mode & 4) != 0;
+  const bool timing = TIMING && (mode & 4) != 0;
   mode &= 3;
   long long tA = 0, tB = 0, tC = 0, tD = 0, t0 = 0;
   const unsigned mbar = tk_smem(&s.mbar);
@@ -832,7 +837,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         if (gb_lane() == 0) k = atomicAdd(&s.sbnext, 1);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= nsb) break;
-        tile_subband(s, op, lpt ? ord[k] : k, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
+        tile_subband<TIMING>(s, op, lpt ? ord[k] : k, nsb, Ny, nA, base, scr, timing ? counter + 24 : nullptr);
       }
     }
     // the bulk copies of phase D (async proxy) read the records written above and overwrite shared
@@ -1007,9 +1012,10 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
 
 void gb_tile_setup(GbCtx& c) {
   c.tile_smem = sizeof(TileSmem);
-  cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.tile_smem);
+  cudaFuncSetAttribute(k_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.tile_smem);
+  cudaFuncSetAttribute(k_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.tile_smem);
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile, TK_NT, c.tile_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<false>, TK_NT, c.tile_smem);
   c.tile_blocks = c.nsm * (per_sm > 0 ? per_sm : 1);
 }
 
@@ -1048,8 +1054,12 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
     c.prof_flags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0;
     cudaEventRecordWithFlags(e0, c.stream, c.prof_flags);
   }
-  k_tile<<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode | (c.timing ? 4 : 0), c.tile_scratch,
-                                                        c.tile_scr_bytes, c.tile_counter, c.st);
+  if (c.timing)
+    k_tile<true><<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode | 4, c.tile_scratch,
+                                                                c.tile_scr_bytes, c.tile_counter, c.st);
+  else
+    k_tile<false><<<c.tile_blocks, TK_NT, c.tile_smem, c.stream>>>(op, A, B, O, g, mode, c.tile_scratch,
+                                                                 c.tile_scr_bytes, c.tile_counter, c.st);
   if (c.prof) cudaEventRecordWithFlags(e1, c.stream, c.prof_flags);
   c.launches += 2;
   if (mode == 0) {
@@ -1246,7 +1256,7 @@ extern "C" int gb_bool_tile_noalloc(int op, const int4* d_A, int nA, const int4*
         fprintf(stderr, "gb_bool_tile_noalloc: cudaGetSymbolAddress failed on device %d\n", dev);
         return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
       }
-      if (cudaFuncSetAttribute(k_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)) !=
+      if (cudaFuncSetAttribute(k_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)) !=
           cudaSuccess)
         return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
       g_na_state_ptr[dev] = (NoAllocState*)a;
@@ -1271,7 +1281,7 @@ extern "C" int gb_bool_tile_noalloc(int op, const int4* d_A, int nA, const int4*
     long long* ctr = S->ctr;
     DStatus* st = &S->res.st;
     void* args[] = {&op, &la, &lb, &lo, &gg, &mode, &scr, &scr_bytes, &ctr, &st};
-    if (cudaLaunchKernel((const void*)k_tile, dim3(1), dim3(TK_NT), args, sizeof(TileSmem), s) != cudaSuccess)
+    if (cudaLaunchKernel((const void*)k_tile<false>, dim3(1), dim3(TK_NT), args, sizeof(TileSmem), s) != cudaSuccess)
       return na_refuse(GB_ERR_CUDA, d_count, d_area, s);
   }
   {
