@@ -352,12 +352,60 @@ __device__ __forceinline__ void emit_box_tiles(DLayer* O, int k, int4 b, long lo
   }
 }
 
+// All 32 lanes call: a box that lies in one tile (nearly all) takes its slot
+// with one atomic per group of lanes that target the same tile (the group's
+// first lane adds the group's size; each lane's slot is its rank in the
+// group), so the pieces of one source tile, which mostly land in one target
+// tile, do not serialise on that tile's counter.  Boxes over several tiles
+// take the per-tile path.  valid = false: the lane places nothing.  Used for
+// binned sources (count 1.71 -> 0.83 ms, scatter 1.93 -> 1.38 ms per two
+// 1024-cell decks); raw sources scatter over many tiles and keep per-lane
+// slots.
+template <int MODE, bool SCATTER>
+__device__ __forceinline__ void emit_warp(DLayer* O, int k, int4 b, long long payload_idx, int g, bool valid) {
+  const int lane = gb_lane();
+  long long t = -1 - lane;  // distinct for lanes without a single tile
+  bool single = false;
+  int tx0 = 0, ty0 = 0;
+  if (valid) {
+    tx0 = gb_floor_shift(b.x, g);
+    ty0 = gb_floor_shift(b.y, g);
+    const int tx1 = MODE ? gb_floor_shift(b.z, g) : gb_floor_shift(b.z - 1, g);
+    const int ty1 = MODE ? gb_floor_shift(b.w, g) : gb_floor_shift(b.w - 1, g);
+    single = tx0 == tx1 && ty0 == ty1;
+    if (single) {
+      const int4 w = O->win[k];
+      t = O->tbase[k] + (long long)(ty0 - w.y) * w.z + (tx0 - w.x);
+    }
+  }
+  const unsigned grp = __match_any_sync(0xffffffffu, t);
+  const int lead = __ffs(grp) - 1;
+  int base = 0;
+  if (single && lane == lead) base = atomicAdd(&O->tcount[t], __popc(grp));
+  base = __shfl_sync(0xffffffffu, base, lead);
+  if (single) {
+    if (SCATTER) {
+      const long long pos = O->tstart[t] + base + __popc(grp & ((1u << lane) - 1u));
+      if (MODE == 0) {
+        const int ox = tx0 << g, oy = ty0 << g;
+        O->pcs[pos] = gb_pack(b.x - ox, b.y - oy, b.z - ox, b.w - oy);
+      } else {
+        ((int*)O->pcs)[pos] = (int)payload_idx;
+      }
+    }
+  } else if (valid) {
+    emit_box_tiles<MODE, SCATTER>(O, k, b, payload_idx, g);
+  }
+}
+
 template <int MODE, bool SCATTER>
 __global__ void k_split_raw(const DLayer* S, DLayer* O, int ncell, int g, int E, int N, int W,
                             int Sg, DStatus* st) {
   if (st->err) return;
   walk_raw_boxes<SCATTER ? 2 : BIN_LD>(S->boxes, S->coff, ncell, S->nbox,
                                        [&](long long i, bool valid_i, int4 box, int k) {
+    // raw boxes of one warp fall in scattered tiles of their cell, so a per-lane slot is cheaper
+    // here than grouping lanes by tile
     int4 b;
     if (!valid_i || !grow_box(box, E, N, W, Sg, b)) return;  // invalid: reported by k_bbox_raw
     emit_box_tiles<MODE, SCATTER>(O, k, b, i, g);
@@ -378,12 +426,16 @@ __global__ void k_split_bin(const DLayer* S, DLayer* O, int g, int E, int N, int
     tile_of_index(S, t, k, tx, ty);
     const unsigned long long* p = S->pcs + S->tstart[t];
     const int ox = tx << sg, oy = ty << sg;
-    for (int j = gb_lane(); j < cnt; j += 32) {
-      int a, b, c, d;
-      gb_unpack(p[j], a, b, c, d);
-      int4 gbx;
-      if (!grow_box(make_int4(ox + a, oy + b, ox + c, oy + d), E, N, W, Sg, gbx)) continue;
-      emit_box_tiles<0, SCATTER>(O, k, gbx, 0, g);
+    for (int j0 = 0; j0 < cnt; j0 += 32) {  // whole warps: emit_warp is a warp collective
+      const int j = j0 + gb_lane();
+      int4 gbx = make_int4(0, 0, 1, 1);
+      bool ok = false;
+      if (j < cnt) {
+        int a, b, c, d;
+        gb_unpack(p[j], a, b, c, d);
+        ok = grow_box(make_int4(ox + a, oy + b, ox + c, oy + d), E, N, W, Sg, gbx);
+      }
+      emit_warp<0, SCATTER>(O, k, gbx, 0, g, ok);
     }
   }
 }
