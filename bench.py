@@ -172,7 +172,7 @@ def P99_TARGET_MS(rate):
     """Stated serving target for the cfg4 layers (64 resident layers with box
     counts across 1k..20M, two of them 20M): p99 latency, arrival to
     completion, of at most 25 ms up to 1000 requests/s.  Above the loop's
-    capacity at these sizes (about 1700 requests/s, 3.6e9 boxes/s measured)
+    capacity at these sizes (about 1900 requests/s, 3.6e9 boxes/s measured)
     the backlog grows for as long as requests keep coming, so no latency
     target can hold there; those rates report the rate actually served
     (target None)."""

@@ -71,6 +71,14 @@ __device__ __forceinline__ int pr_hrank(const PieceRec& p) {
   return (int)(((unsigned)p.y >> 17) | (((unsigned)p.z >> 17) << 15));
 }
 
+// A tile to process: its index, cell and the two operands' pieces.
+struct TileRef {
+  long long tile;
+  const unsigned long long* pa;
+  const unsigned long long* pb;
+  int nA, nB, cell, pad;
+};
+
 struct TileSmem {
   union {  // phases A-B: value bitmaps and their prefix popcounts; phase D: x / y value tables
     struct {
@@ -100,6 +108,8 @@ struct TileSmem {
   const unsigned long long* pa;
   const unsigned long long* pb;
   int nA, nB, cell, err;
+  TileRef nx;   // the next tile, reserved and looked up during this tile's phase D
+  int have_nx;
   long long obase;
   DStatus* st;
   unsigned long long up, down;  // scratch bump: bytes (low half) / 32-byte records (high half)
@@ -200,6 +210,35 @@ __device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long lo
   return base + off;
 }
 
+
+// Output tile t: its cell, and where A's and B's pieces of that tile start.
+__device__ __forceinline__ void tile_lookup(int op, const DLayer* A, const DLayer* B, const DLayer* O, long long t,
+                                            TileRef& r) {
+  r.tile = t;
+  r.nA = r.nB = 0;
+  r.pa = r.pb = nullptr;
+  r.cell = 0;
+  if (t >= O->ntiles) return;
+  const int k = gb_find_cell(O->tbase, O->ncell, t);
+  const int4 w = O->win[k];
+  const long long li = t - O->tbase[k];
+  const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+  r.cell = k;
+  const int4 wa = A->win[k];
+  if (tx >= wa.x && ty >= wa.y && tx < wa.x + wa.z && ty < wa.y + wa.w) {
+    const long long ta = A->tbase[k] + (long long)(ty - wa.y) * wa.z + (tx - wa.x);
+    r.nA = A->tcount[ta];
+    r.pa = A->pcs + A->tstart[ta];
+  }
+  if (B && op != GB_OP_MERGE && op != GB_OP_OVERLAP) {
+    const int4 wb = B->win[k];
+    if (tx >= wb.x && ty >= wb.y && tx < wb.x + wb.z && ty < wb.y + wb.w) {
+      const long long tb = B->tbase[k] + (long long)(ty - wb.y) * wb.z + (tx - wb.x);
+      r.nB = B->tcount[tb];
+      r.pb = B->pcs + B->tstart[tb];
+    }
+  }
+}
 
 // TIMING: the phase counters of gb_tile_timing are compiled in (tctr non-null
 // then); the production instance has none of that code.
@@ -564,39 +603,27 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s.have_nx = 0;
   }
   for (;;) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // before this tile's bulk copies
     __syncthreads();
     if (tid == 0) {
       s.st = st;
-      s.tile = st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull);
-      s.nA = s.nB = 0;
+      TileRef r;
+      if (s.have_nx) r = s.nx;
+      else tile_lookup(op, A, B, O, st->err ? (1ll << 62) : (long long)atomicAdd((unsigned long long*)counter, 1ull), r);
+      s.have_nx = 0;
+      if (st->err) r.tile = 1ll << 62;  // an error stops the CTA, a reserved tile too
+      s.tile = r.tile;
+      s.nA = r.nA;
+      s.nB = r.nB;
+      s.pa = r.pa;
+      s.pb = r.pb;
+      s.cell = r.cell;
       s.up = 0;
       s.down = 0;
       s.err = 0;
-      const long long t = s.tile;
-      if (t < O->ntiles) {
-        const int k = gb_find_cell(O->tbase, O->ncell, t);
-        const int4 w = O->win[k];
-        const long long li = t - O->tbase[k];
-        const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
-        s.cell = k;
-        const int4 wa = A->win[k];
-        if (tx >= wa.x && ty >= wa.y && tx < wa.x + wa.z && ty < wa.y + wa.w) {
-          const long long ta = A->tbase[k] + (long long)(ty - wa.y) * wa.z + (tx - wa.x);
-          s.nA = A->tcount[ta];
-          s.pa = A->pcs + A->tstart[ta];
-        }
-        if (B && op != GB_OP_MERGE && op != GB_OP_OVERLAP) {
-          const int4 wb = B->win[k];
-          if (tx >= wb.x && ty >= wb.y && tx < wb.x + wb.z && ty < wb.y + wb.w) {
-            const long long tb = B->tbase[k] + (long long)(ty - wb.y) * wb.z + (tx - wb.x);
-            s.nB = B->tcount[tb];
-            s.pb = B->pcs + B->tstart[tb];
-          }
-        }
-      }
     }
     __syncthreads();
     const long long t = s.tile;
@@ -864,6 +891,12 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         gb_set_error(st, GB_ERR_CAPACITY, KID_TILE, (long long)scr * 2);
       }
       continue;
+    }
+    // the next tile's reservation and lookups (a chain of dependent loads) run on the last thread while
+    // the others stitch and emit this tile
+    if (tid == TK_NT - 1 && !st->err) {
+      tile_lookup(op, A, B, O, (long long)atomicAdd((unsigned long long*)counter, 1ull), s.nx);
+      s.have_nx = 1;
     }
     PieceRec* PR = prs ? reinterpret_cast<PieceRec*>(s.dbuf) : nullptr;
     int* succ = prs ? reinterpret_cast<int*>(s.dbuf + (size_t)NP * 16) : s.succ;
