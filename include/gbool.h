@@ -392,11 +392,14 @@ int gb_profile(gb_context* ctx, int on);
 int gb_profile_read(gb_context* ctx, double* ms_total, long long* launches, long long* bytes_in,
                     long long* bytes_out);
 long long gb_launch_count(gb_context* ctx);
-/* Diagnostics: per-phase cycle counters of the scanline kernel.  out8 (16
- * entries, 24 with the raster sub-steps) gets cycles of phases A (ranks), B (sub-band lists), C (sub-band
+/* Diagnostics: per-phase cycle counters of the scanline kernel.  out8 (40
+ * entries) gets cycles of phases A (ranks), B (sub-band lists), C (sub-band
  * sweeps), D (stitch/emit) summed over CTAs; tiles, pieces, sub-bands, strip
- * pieces; then per-warp cycles of the sub-band steps (compress, rasterise,
- * scan, count, write), members and columns, since gb_tile_timing(ctx, 1). */
+ * pieces; then 16 per-warp counters of the sub-band steps (compress,
+ * rasterise, scan, count, write, transpose cycles, members, columns); then
+ * per sub-band-count bucket (1, 2-3, 4-7, 8-15, 16-31, 32+) the tiles and
+ * their phase-C cycles; the sub-bands whose column words spilled to scratch
+ * and their cycles, the others and theirs; all since gb_tile_timing(ctx, 1). */
 int gb_tile_timing(gb_context* ctx, int on);
 /* Diagnostics: runs one radix pass whose only CTA waits for a predecessor
  * tile that never publishes; returns the status it reports (GB_ERR_TIMEOUT

@@ -76,9 +76,12 @@ extern "C" int gb_profile_read(gb_context* ctx, double* ms_total, long long* lau
 
 // Per-phase cycle counters of the scanline kernel (diagnostics): on != 0
 // enables them; gb_tile_timing_read returns [cycA, cycB, cycC, cycD, tiles,
-// pieces, sub-bands, strip pieces] summed over CTAs since enabling.
+// pieces, sub-bands, strip pieces] summed over CTAs since enabling, the
+// sub-band step counters, per sub-band-count bucket the tiles and their
+// phase-C cycles, and the sub-bands with and without spilled column words and
+// their cycles (40 values).
 __global__ void k_zero_timing(long long* ctr) {
-  for (int i = 16; i < 40; ++i) ctr[i] = 0;
+  for (int i = 16; i < 56; ++i) ctr[i] = 0;
 }
 extern "C" int gb_tile_timing(gb_context* ctx, int on) {
   if (!ctx) return GB_ERR_ARG;
@@ -89,7 +92,7 @@ extern "C" int gb_tile_timing(gb_context* ctx, int on) {
 extern "C" int gb_tile_timing_read(gb_context* ctx, long long* out8) {
   if (!ctx || !out8) return GB_ERR_ARG;
   cudaStreamSynchronize(ctx->c.stream);
-  cudaMemcpy(out8, ctx->c.tile_counter + 16, 24 * sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaMemcpy(out8, ctx->c.tile_counter + 16, 40 * sizeof(long long), cudaMemcpyDeviceToHost);
   return GB_OK;
 }
 

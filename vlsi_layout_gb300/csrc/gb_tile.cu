@@ -248,6 +248,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   if (!TIMING) tctr = nullptr;
   const int lane = gb_lane(), wid = gb_warp();
   long long q0 = tctr ? clock64() : 0;
+  const long long qstart = q0;
 #define TSTEP(k) if (tctr && lane == 0) { const long long q1 = clock64(); atomicAdd((unsigned long long*)&tctr[k], (unsigned long long)(q1 - q0)); q0 = q1; }
   const unsigned long long half = scr >> 1;
   const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
@@ -402,6 +403,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   // No region in rows 1..63: the sub-band has no strip pieces (row 0 belongs to
   // the previous sub-band, and its runs matter only to continuations here).
   if (!__any_sync(0xffffffffu, (rany & ~1ull) != 0ull)) {
+    TSTEP(1)
     if (lane == 0) {
       s.sbinfo[sb] = make_int4(0, 0, 0, 0);
       s.sbh[sb] = 0;
@@ -575,6 +577,11 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     }
   }
   TSTEP(4)
+  if (tctr && lane == 0) {  // sub-bands whose column words spilled to scratch: count and cycles
+    const long long q1 = clock64();
+    atomicAdd((unsigned long long*)&tctr[28 + (L > TK_LCN ? 0 : 2)], 1ull);
+    atomicAdd((unsigned long long*)&tctr[29 + (L > TK_LCN ? 0 : 2)], (unsigned long long)(q1 - qstart));
+  }
   if (lane == 0) {
     s.sbinfo[sb] = make_int4(pbase, totP, totO, 0);
     s.sbol[sb] = (int*)obase;
@@ -872,7 +879,16 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     asm volatile("fence.proxy.async.global;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (timing) { const long long t1 = clock64(); tC += t1 - t0; t0 = t1; }
+    if (timing) {
+      const long long t1 = clock64();
+      tC += t1 - t0;
+      if (tid == 0) {  // phase C per tile, by the tile's sub-band count: 1, 2-3, 4-7, 8-15, 16-31, 32+
+        const int bk = nsb <= 1 ? 0 : nsb <= 3 ? 1 : nsb <= 7 ? 2 : nsb <= 15 ? 3 : nsb <= 31 ? 4 : 5;
+        atomicAdd((unsigned long long*)&counter[40 + bk], 1ull);
+        atomicAdd((unsigned long long*)&counter[46 + bk], (unsigned long long)(t1 - t0));
+      }
+      t0 = t1;
+    }
     // ---- D: stitch and emit.  Piece records, chain links and the x / y value
     // tables are staged in shared memory that phases A-C no longer use.
     const int NP = (int)s.down;
