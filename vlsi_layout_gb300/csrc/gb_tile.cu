@@ -53,6 +53,9 @@
 #define TK_LCN 128
 #define TK_MW 64
 #define TK_LD 2     // independent global loads in flight per thread in the streaming loops
+#define TK_DIRECT 1 // columns of a member painted on its own lane; the rest are spread over the warp
+                    // (measured per 1024-cell deck: 0 / 1 / 2 / 3 / 4 / 8 columns -> 35.16 / 34.78 /
+                    // 34.91 / 34.85 / 35.02 / 38.13 ms)
 #define KID_TILE 20
 
 // A strip piece of one sub-band, 16 bytes, stored downward from the top of
@@ -342,11 +345,11 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       lc1 = bm_rank(lb, lp, r.z);
       span = bm_rank(lb, lp, r.w) - lc1;
     }
-    // direct: the first 4 columns of every member on its own lane
+    // direct: the first TK_DIRECT columns of every member on its own lane
     {
       unsigned* col = (unsigned*)(own ? cb : ca);
       const unsigned mlo = (unsigned)mk, mhi = (unsigned)(mk >> 32);
-      const int d = min(span, 4);
+      const int d = min(span, TK_DIRECT);
       if (op == GB_OP_OVERLAP) {
         for (int c = lc1; c < lc1 + d; ++c) paint_twice((unsigned*)ca, (unsigned*)cb, c, mlo, mhi);
       } else {
@@ -358,7 +361,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     }
     if (tctr) { const long long qb = clock64(); qsetup += qb - qa; qa = qb; }
     // remainder of long members: (member, column) pairs spread over the lanes
-    const int rest = max(span - 4, 0);
+    const int rest = max(span - TK_DIRECT, 0);
     if (__any_sync(0xffffffffu, rest > 0)) {
       const int incl = gb_warp_incl(rest);
       const int total = __shfl_sync(0xffffffffu, incl, 31);
@@ -377,7 +380,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         const unsigned long long mk_o = __shfl_sync(0xffffffffu, mk, o);
         if (k < total) {
           unsigned* col = (unsigned*)(own_o ? cb : ca);
-          const int c = c1_o + 4 + (k - ex_o);
+          const int c = c1_o + TK_DIRECT + (k - ex_o);
           if (op == GB_OP_OVERLAP) {
             paint_twice((unsigned*)ca, (unsigned*)cb, c, (unsigned)mk_o, (unsigned)(mk_o >> 32));
           } else {
