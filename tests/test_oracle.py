@@ -248,3 +248,29 @@ def test_refpath_op1_point_sets(oracle, n, die, seed):
     off = np.array([0, n], np.int64)
     counts, area = oracle.refpath_op1_cells(A, off)
     assert counts[0, 4] == 0 and counts[0, 5] == 0 and area[0] == oracle.union_area(A)
+
+
+def test_strip_digest_formula(oracle):
+    """The per-cell strip digest (gb_layer_digest on the device, orc_strip_digest
+    in the oracle) is the sum mod 2^64 of fmix64((x1<<32|y1) ^ fmix64((x2<<32|y2)
+    + 0x9e3779b97f4a7c15)) over the strips, coordinates as uint32; it does not
+    depend on the strip order."""
+    M = (1 << 64) - 1
+
+    def fmix(k):
+        k ^= k >> 33
+        k = (k * 0xff51afd7ed558ccd) & M
+        k ^= k >> 33
+        k = (k * 0xc4ceb9fe1a85ec53) & M
+        return k ^ (k >> 33)
+
+    def h(x1, y1, x2, y2):
+        u = ((x1 & 0xffffffff) << 32) | (y1 & 0xffffffff)
+        v = ((x2 & 0xffffffff) << 32) | (y2 & 0xffffffff)
+        return fmix(u ^ fmix((v + 0x9e3779b97f4a7c15) & M))
+
+    b = random_layer(500, die=40000, seed=71, x0=-20000)
+    assert oracle.strip_digest(b) == sum(h(*map(int, r)) for r in b) & M
+    assert oracle.strip_digest(b[::-1]) == oracle.strip_digest(b)
+    assert oracle.strip_digest(b[:0]) == 0
+    assert oracle.lib().orc_strip_hash(-1, 2, 3, -4) == h(-1, 2, 3, -4)
