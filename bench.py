@@ -576,8 +576,23 @@ def events_leg(n=50_000_000, steps=2):
     ref = t[order]
     ok = all(np.array_equal(o[f], ref[f]) for o in (out, dout) for f in ("X", "Y", "polygonNumber"))
     sh, sd = statistics.median(th), statistics.median(td)
+    # algorithmic bytes per tracker of the device-array call: key generation 12 read + 12 written, key span 8,
+    # the sort's histogram read 8 and P passes of key + payload read and written (24 each), gather 4 + 12 read and
+    # 12 written, copy back 12 + 12
+    kx = keys(t)
+    bits = int(np.bitwise_or.reduce(kx ^ kx[0])).bit_length()
+    import ctypes
+    passes, tile = ctypes.c_int(), ctypes.c_int()
+    L.gb_radix_plan(torch.cuda.current_device(), bits, n, ctypes.byref(passes), ctypes.byref(tile))
+    per = 24 + 8 + 8 + 24 * passes.value + 28 + 24
+    peak, peak_kind = peaks()
+    gbs = n * per / sd / 1e9
     return {"n": n, "host_s": sh, "host_trackers_per_s": n / sh, "device_s": sd, "device_trackers_per_s": n / sd,
             "sorted_equal_numpy_stable": ok,
+            "roofline": {"bound": "hbm", "key_bits": bits, "passes": passes.value, "bytes_per_tracker": per,
+                         "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "note": "device-array call, wall clock; includes the call's temporary allocations "
+                                 "(%.2f GB) and its stream synchronisations" % (n * 36 / 1e9)},
             "check": "host- and device-array outputs equal numpy's stable sort of the input by the packed key, "
                      "X, Y and polygonNumber",
             "timing": "host wall clock around device_event_sort (host array: H2D + D2H inside; device array)",

@@ -221,6 +221,11 @@ int gb_radix_autotune(gb_context* ctx, const unsigned long long* d_keys, const u
                       int bits, int* passes, int* tile, float* ms);
 /* Clear the autotuner's table (later sorts use the default again). */
 void gb_radix_tuning_reset(void);
+/* The plan (pass count, keys per tile) the device sort takes for `bits`
+ * significant key bits and n keys on `device`: the tuned one for that bit
+ * width and size class, else the default (fewest passes of at most 7 bits,
+ * rounded up to an even count; 8192-key tiles).  For byte accounting. */
+int gb_radix_plan(int device, int bits, long long n, int* passes, int* tile);
 /* Morton keys of device boxes (gpu_morton.cu:113-144) and the identity
  * permutation, on the device. */
 int gb_morton_keys_device(gb_context* ctx, const c_box* d_boxes, long long n, unsigned long long* d_keys,

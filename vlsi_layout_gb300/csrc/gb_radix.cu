@@ -607,6 +607,26 @@ void gb_radix_free(GbCtx& c) {
 // passes with digits of at most 7 bits (radix <= RS_AO_RADIX ranks through
 // shared lane masks), one more when that makes the count even (it moves as
 // many bytes as the final copy it saves), tiles of 8192 keys.
+// The plan gb_radix_sort_pairs takes for `bits` significant bits and n keys
+// on `device`: the tuned one for that bit width and size class, else the
+// default.
+extern "C" int gb_radix_plan(int device, int bits, long long n, int* passes, int* tile) {
+  if (!passes || !tile || bits < 1 || bits > 64 || n < 1) return GB_ERR_ARG;
+  int tp = 0, ti = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto f = g_tuned.find(std::make_tuple(device, bits, log2_bucket(n)));
+    if (f != g_tuned.end()) {
+      tp = f->second.first;
+      ti = f->second.second;
+    }
+  }
+  if (!tp) gb_radix_default(bits, &tp, &ti);
+  *passes = std::min(tp, bits);
+  *tile = ti;
+  return GB_OK;
+}
+
 void gb_radix_default(int bits, int* passes, int* tile) {
   int p = (bits + 6) / 7;
   if ((p & 1) && p + 1 <= bits) ++p;

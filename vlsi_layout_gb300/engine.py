@@ -88,6 +88,7 @@ def lib():
         "gb_op1_host": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P]),
         "gb_op1_host_digest": (ctypes.c_int, [P, P, u64, P, ctypes.c_int, i32, P, P, P, P]),
         "gb_layer_digest": (ctypes.c_int, [P, P, P]),
+        "gb_radix_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, i64, P, P]),
         "gb_op1_area": (ctypes.c_int, [P, P, i32, P, P]),
         "gb_graph_begin": (ctypes.c_int, [P]),
         "gb_graph_end": (ctypes.c_int, [P, pp]),
