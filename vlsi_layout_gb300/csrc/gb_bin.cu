@@ -551,8 +551,18 @@ __global__ void k_bool_window(int op, const DLayer* A, const DLayer* B, DLayer* 
     }
     O->tstart = (long long*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 8, KID_ALLOC);
     O->tcount = (int*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 4, KID_ALLOC);
-    if (!O->tstart || !O->tcount) O->ntiles = 0;
+    O->tcell = (int*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 4, KID_ALLOC);
+    if (!O->tstart || !O->tcount || !O->tcell) O->ntiles = 0;
   }
+}
+
+// Cell of every output tile, so the tile kernel finds a tile's cell with one
+// load instead of a binary search of tbase.
+__global__ void k_tile_cells(DLayer* O, DStatus* st) {
+  if (st->err) return;
+  const long long n = O->ntiles;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    O->tcell[t] = gb_find_cell(O->tbase, O->ncell, t);
 }
 
 // Output pool of a Boolean op: factor x (pieces of A + pieces of B) plus a
@@ -573,6 +583,7 @@ __global__ void k_pool_alloc(const DLayer* A, const DLayer* B, DLayer* O, int fa
 void gb_launch_bool_setup(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int ncell,
                           int g, int alloc_slots) {
   k_bool_window<<<1, 1024, 0, c.stream>>>(op, A, B, O, ncell, g, c.st);
+  k_tile_cells<<<c.work_blocks, 256, 0, c.stream>>>(O, c.st);
   if (!alloc_slots) return;
   k_pool_alloc<<<1, 1, 0, c.stream>>>(A, op == GB_OP_MERGE ? nullptr : B, O, c.cap_factor, c.st);
 }

@@ -74,6 +74,7 @@ struct DLayer {
   long long nused;         // pool cursor (Boolean results reserve per tile from it)
   long long ntot;          // pieces held by the layer
   int4* cbox;              // [ncell] bounding box (raw and binned)
+  int* tcell;              // [ntiles] cell of each tile (Boolean results; null elsewhere: search tbase)
 };
 
 __host__ __device__ inline unsigned long long gb_pack(int x1, int y1, int x2, int y2) {

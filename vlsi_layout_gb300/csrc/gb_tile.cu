@@ -27,11 +27,17 @@
 //     scan) delivers that OR at each run's last column for all 64 rows at
 //     once.  A strip piece starts wherever the run changed; it ends at the
 //     next change.  Pieces reaching row 63 are "open", pieces starting at
-//     row 1 with no change from row 0 are "continuations".
-//  D. Stitch.  Each continuation is linked to the open piece of the previous
-//     sub-band with the same y-interval; every chain head becomes one strip.
-//     Strips are written in (sub-band, column, row) order, so the output of a
-//     tile is deterministic.
+//     row 1 with no change from row 0 are "continuations".  The scan pass
+//     leaves each column's local prefix of the recurrence, the count pass
+//     each column's piece starts, so the passes after them do not evaluate
+//     it again.  A piece's 16-byte record goes to the CTA's record region at
+//     the piece's index.
+//  D. Stitch.  The records come into shared memory in one bulk copy.  Each
+//     continuation is linked to the open piece of the previous sub-band with
+//     the same y-interval; every chain head becomes one strip.  The output
+//     slots are reserved while the links are made.  Strips are written in
+//     (sub-band, column, row) order, so the output of a tile is
+//     deterministic.
 // No CTA ever waits on another CTA.  The only waits are on the CTA's own
 // mbarrier for the bulk copies of phases A and D; each is bounded (a poll
 // limit, then GB_ERR_TIMEOUT and the CTA leaves after its copies land).
@@ -51,7 +57,8 @@
 #define TK_LBW 128
 #define TK_LVN 256
 #define TK_LCN 128
-#define TK_MW 64
+#define TK_MC 128   // sub-band members kept in the per-warp member cache (8 bytes each)
+#define TK_MLD 4    // member records loaded per lane before the first is used
 #define TK_LD 2     // independent global loads in flight per thread in the streaming loops
 #define TK_DIRECT 1 // columns of a member painted on its own lane; the rest are spread over the warp
                     // (measured per 1024-cell deck: 0 / 1 / 2 / 3 / 4 / 8 columns -> 35.16 / 34.78 /
@@ -98,7 +105,9 @@ struct TileSmem {
       int lv[TK_NW][TK_LVN];
       unsigned long long ca[TK_NW][TK_LCN];
       unsigned long long cb[TK_NW][TK_LCN];
-      int4 mc[TK_NW][TK_MW];                  // member cache: slab range (owner bit 31), y ranks
+      // member cache: first row | end row << 7 | owner << 14 | y1 rank << 15, y2 rank << 32 (rows 0..64,
+      // ranks below 2^17)
+      unsigned long long mc[TK_NW][TK_MC];
       unsigned srow[TK_NW][64][TK_LCN / 32];  // run starts, row-major (transposed)
     };
     unsigned char dbuf[1];
@@ -111,11 +120,14 @@ struct TileSmem {
   const unsigned long long* pa;
   const unsigned long long* pb;
   int nA, nB, cell, err;
+  int rsplit;  // some sub-band's piece records did not fit the record region (allocated below instead)
   TileRef nx;   // the next tile, reserved and looked up during this tile's phase D
   int have_nx;
   long long obase;
   DStatus* st;
-  unsigned long long up, down;  // scratch bump: bytes (low half) / 32-byte records (high half)
+  // up: bytes allocated from the lower half of the scratch; down: strip pieces so far, whose records sit at
+  // their piece index in the upper half (the record region)
+  unsigned long long up, down;
   int* Xt;
   int* Yt;
   int4* rk;
@@ -222,7 +234,7 @@ __device__ __forceinline__ void tile_lookup(int op, const DLayer* A, const DLaye
   r.pa = r.pb = nullptr;
   r.cell = 0;
   if (t >= O->ntiles) return;
-  const int k = gb_find_cell(O->tbase, O->ncell, t);
+  const int k = O->tcell ? O->tcell[t] : gb_find_cell(O->tbase, O->ncell, t);
   const int4 w = O->win[k];
   const long long li = t - O->tbase[k];
   const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
@@ -270,14 +282,30 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int nwy = ((Ny - 1) >> 5) + 1;
   unsigned* lb = nwy <= TK_LBW ? s.lb[wid] : s.biglb + (size_t)wid * 2 * nwy;
   unsigned* lp = nwy <= TK_LBW ? s.lp[wid] : lb + nwy;
-  const bool cache = m <= TK_MW;
+  const bool cache = m <= TK_MC;
   for (int w = lane; w < nwy; w += 32) lb[w] = 0;
   __syncwarp();
-  for (int j = lane; j < m; j += 32) {
-    const int4 r = s.mem[beg + j];
-    if (cache) s.mc[wid][j] = r;
-    atomicOr(&lb[r.z >> 5], 1u << (r.z & 31));
-    atomicOr(&lb[r.w >> 5], 1u << (r.w & 31));
+  for (int j0 = 0; j0 < m; j0 += 32 * TK_MLD) {
+    int4 rr[TK_MLD];
+#pragma unroll
+    for (int u = 0; u < TK_MLD; ++u) {
+      const int j = j0 + u * 32 + lane;
+      rr[u] = j < m ? s.mem[beg + j] : make_int4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < TK_MLD; ++u) {
+      const int j = j0 + u * 32 + lane;
+      if (j < m) {
+        const int4 r = rr[u];
+        if (cache) {
+          const unsigned lo = (unsigned)max((r.x & 0x7fffffff) - rowbase, 0), hi = (unsigned)min(r.y - rowbase, 64);
+          s.mc[wid][j] = (unsigned long long)(lo | (hi << 7) | (((unsigned)r.x >> 31) << 14) | ((unsigned)r.z << 15)) |
+                         ((unsigned long long)(unsigned)r.w << 32);
+        }
+        atomicOr(&lb[r.z >> 5], 1u << (r.z & 31));
+        atomicOr(&lb[r.w >> 5], 1u << (r.w & 31));
+      }
+    }
   }
   __syncwarp();
   int nl;
@@ -337,13 +365,26 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
     int lc1 = 0, span = 0, own = 0;
     unsigned long long mk = 0;
     if (j < m) {
-      int4 r = cache ? s.mc[wid][j] : s.mem[beg + j];
-      own = (r.x >> 31) & 1;
-      r.x &= 0x7fffffff;
-      const int lo = max(r.x - rowbase, 0), hi = min(r.y - rowbase, 64);
+      int lo, hi, yz, yw;
+      if (cache) {
+        const unsigned long long e = s.mc[wid][j];
+        const unsigned e0 = (unsigned)e;
+        lo = (int)(e0 & 127u);
+        hi = (int)((e0 >> 7) & 127u);
+        own = (int)((e0 >> 14) & 1u);
+        yz = (int)(e0 >> 15);
+        yw = (int)(e >> 32);
+      } else {
+        const int4 r = s.mem[beg + j];
+        own = (r.x >> 31) & 1;
+        lo = max((r.x & 0x7fffffff) - rowbase, 0);
+        hi = min(r.y - rowbase, 64);
+        yz = r.z;
+        yw = r.w;
+      }
       mk = (hi >= 64 ? ~0ull : ((1ull << hi) - 1ull)) & (~0ull << lo);
-      lc1 = bm_rank(lb, lp, r.z);
-      span = bm_rank(lb, lp, r.w) - lc1;
+      lc1 = bm_rank(lb, lp, yz);
+      span = bm_rank(lb, lp, yw) - lc1;
     }
     // direct: the first TK_DIRECT columns of every member on its own lane
     {
@@ -462,6 +503,7 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
       const unsigned long long b = Rc & Rm1;
       FA = a | (b & FA);
       FB = b & FB;
+      cb[c] = FA;  // local prefix: F_c = FA_c | (FB_c & carry-in)
       Rm1 = Rc;
     }
   }
@@ -480,15 +522,15 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   // ---- count pieces / opens / heads
   int np = 0, no = 0, nh = 0, ncn = 0, nz = 0;
   {
-    unsigned long long Rm1 = R(c0 - 1), F = Fin;
+    unsigned long long Rm1 = R(c0 - 1), fb = ~0ull;
     for (int c = c0; c < c1e; ++c) {
       const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
-      const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
-      const unsigned long long a = Rc & (vchg(Rc) | (Sc & vchg(Rm1)));
-      const unsigned long long b = Rc & Rm1;
-      F = a | (b & F);
+      const unsigned long long Ec = Rc & ~Rp1;
+      fb &= Rc & Rm1;
+      const unsigned long long F = cb[c] | (fb & Fin);
       const unsigned long long Chg = (F | vchg(Rp1)) & Ec;
       const unsigned long long Z = (Chg | 2ull) & Ec & ~1ull;
+      cb[c] = Z | ((Chg >> 1) & 1ull);  // bit 0 of Z is always clear
       const int pc = __popcll(Z);
       np += pc;
       if (!last_sb && (Ec >> 63)) ++no;
@@ -512,7 +554,15 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   if (lane == 0) {
     pbase = (int)atomicAdd(&s.down, (unsigned long long)totP);
     if (totP > 0) {
-      void* p = sc_up(s, base, half, (unsigned long long)totP * sizeof(PieceRec));
+      // the record region is the upper half of the scratch, indexed by piece
+      const unsigned long long rh = half & ~15ull;
+      void* p;
+      if ((unsigned long long)(pbase + totP) * sizeof(PieceRec) <= scr - rh) {
+        p = base + rh + (size_t)pbase * sizeof(PieceRec);
+      } else {
+        p = sc_up(s, base, half, (unsigned long long)totP * sizeof(PieceRec));
+        s.rsplit = 1;
+      }
       rbase = (unsigned long long)p;
       if (!p) pbase = -1;
     }
@@ -532,16 +582,13 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
 
   // ---- write pieces
   {
-    unsigned long long Rm1 = R(c0 - 1), F = Fin;
     int p = pbase + posP, o = posO, h = posH, q = posC, z = posZ;
     for (int c = c0; c < c1e; ++c) {
       const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
-      const unsigned long long Sc = Rc & ~Rm1, Ec = Rc & ~Rp1;
-      const unsigned long long a = Rc & (vchg(Rc) | (Sc & vchg(Rm1)));
-      const unsigned long long b = Rc & Rm1;
-      F = a | (b & F);
-      const unsigned long long Chg = (F | vchg(Rp1)) & Ec;
-      const unsigned long long Z = (Chg | 2ull) & Ec & ~1ull;
+      const unsigned long long Ec = Rc & ~Rp1;
+      const unsigned long long zs = cb[c];
+      const unsigned long long Z = zs & ~1ull;
+      const unsigned long long Chg = zs << 1;  // only its bit 1 is read below
       unsigned long long Zr = Z;
       while (Zr) {
         const int r = __ffsll((long long)Zr) - 1;
@@ -576,7 +623,6 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
         ++p;
       }
       z += (int)(Ec & 1ull);
-      Rm1 = Rc;
     }
   }
   TSTEP(4)
@@ -634,6 +680,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       s.up = 0;
       s.down = 0;
       s.err = 0;
+      s.rsplit = 0;
     }
     __syncthreads();
     const long long t = s.tile;
@@ -717,7 +764,7 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
     __syncthreads();
     int Nx, Ny;
     {
-      const int per = ((W + TK_NT - 1) / TK_NT + 3) & ~3, w0 = min(W, tid * per), w1 = min(W, w0 + per);
+      const int per = ((W + TK_NT - 1) / TK_NT) | 1, w0 = min(W, tid * per), w1 = min(W, w0 + per);
       long long cx = 0, cy = 0;
       for (int w = w0; w < w1; ++w) { cx += __popc(s.xb[w]); cy += __popc(s.yb[w]); }
       long long tot;
@@ -937,11 +984,14 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
           if (ny4) tk_bulk(s.xyv + xyoff + nx4, s.Yt, (unsigned)ny4 * 4u, mbar);
         }
       }
-      if (prs && wid == 0)
+      if (prs && !s.rsplit) {
+        if (tid == 0 && NP > 0) tk_bulk(PR, base + (half & ~15ull), (unsigned)NP * 16u, mbar);
+      } else if (prs && wid == 0) {
         for (int sb = lane; sb < nsb; sb += 32) {
           const int4 inf = s.sbinfo[sb];
           if (inf.y > 0) tk_bulk(PR + inf.x, s.sbrec[sb], (unsigned)inf.y * 16u, mbar);
         }
+      }
       const bool ok = tk_wait(mbar, mph, TK_SPIN_LIMIT);
       mph ^= 1u;
       if (__syncthreads_or(!ok)) {
@@ -965,6 +1015,20 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       H = (int)carry;
     }
     __syncthreads();
+    if (tid == TK_NT - 32) {  // read after the links' barrier
+      s.obase = -1;
+      if (mode == 0 && H > 0) {
+        atomicAdd((unsigned long long*)&O->ntot, (unsigned long long)H);
+        const long long o = (long long)atomicAdd((unsigned long long*)&O->nused, (unsigned long long)H);
+        if (o + H <= O->npcs) {
+          s.obase = o;
+        } else {
+          unsigned long long* p =
+              (unsigned long long*)gb_arena_alloc_atomic(st, (unsigned long long)H * 8ull, KID_TILE + 1);
+          if (p) s.obase = (long long)(p - O->pcs);
+        }
+      }
+    }
     // link every continuation piece to the open piece of the previous
     // sub-band: its row-0 ordinal indexes that sub-band's open list directly
     for (int sb = 1 + wid; sb < nsb; sb += TK_NW) {
@@ -978,21 +1042,6 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
         const int ord = pr_hrank(REC(sb, p));
         if (ord < pinf.z) succ[ol[ord]] = p;
         else gb_set_error(st, GB_ERR_INTERNAL, KID_TILE, t);
-      }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      s.obase = -1;
-      if (mode == 0 && H > 0) {
-        atomicAdd((unsigned long long*)&O->ntot, (unsigned long long)H);
-        const long long o = (long long)atomicAdd((unsigned long long*)&O->nused, (unsigned long long)H);
-        if (o + H <= O->npcs) {
-          s.obase = o;
-        } else {
-          unsigned long long* p =
-              (unsigned long long*)gb_arena_alloc_atomic(st, (unsigned long long)H * 8ull, KID_TILE + 1);
-          if (p) s.obase = (long long)(p - O->pcs);
-        }
       }
     }
     __syncthreads();
