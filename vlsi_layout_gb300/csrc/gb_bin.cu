@@ -551,18 +551,37 @@ __global__ void k_bool_window(int op, const DLayer* A, const DLayer* B, DLayer* 
     }
     O->tstart = (long long*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 8, KID_ALLOC);
     O->tcount = (int*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 4, KID_ALLOC);
-    O->tcell = (int*)gb_arena_alloc(st, (unsigned long long)(total + 1) * 4, KID_ALLOC);
-    if (!O->tstart || !O->tcount || !O->tcell) O->ntiles = 0;
+    O->tdesc = (TileDesc*)gb_arena_alloc(st, (unsigned long long)(total + 1) * sizeof(TileDesc), KID_ALLOC);
+    if (!O->tstart || !O->tcount || !O->tdesc) O->ntiles = 0;
   }
 }
 
-// Cell of every output tile, so the tile kernel finds a tile's cell with one
-// load instead of a binary search of tbase.
-__global__ void k_tile_cells(DLayer* O, DStatus* st) {
+// Every output tile's cell and the operands' pieces of that tile, so the tile
+// kernel looks a tile up with one load.  Only B's pieces of a two-operand op.
+__global__ void k_tile_descs(int op, const DLayer* A, const DLayer* B, DLayer* O, DStatus* st) {
   if (st->err) return;
   const long long n = O->ntiles;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-    O->tcell[t] = gb_find_cell(O->tbase, O->ncell, t);
+  const bool useB = B && op != GB_OP_MERGE && op != GB_OP_OVERLAP;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int k = gb_find_cell(O->tbase, O->ncell, t);
+    const int4 w = O->win[k];
+    const long long li = t - O->tbase[k];
+    const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
+    TileDesc d;
+    d.cell = k;
+    d.nA = d.nB = d.pad = 0;
+    d.offA = d.offB = 0;
+    long long ta = 0, tb = 0;
+    if (tile_index_in(A, k, tx, ty, &ta)) {
+      d.nA = A->tcount[ta];
+      d.offA = A->tstart[ta];
+    }
+    if (useB && tile_index_in(B, k, tx, ty, &tb)) {
+      d.nB = B->tcount[tb];
+      d.offB = B->tstart[tb];
+    }
+    O->tdesc[t] = d;
+  }
 }
 
 // Output pool of a Boolean op: factor x (pieces of A + pieces of B) plus a
@@ -583,7 +602,7 @@ __global__ void k_pool_alloc(const DLayer* A, const DLayer* B, DLayer* O, int fa
 void gb_launch_bool_setup(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLayer* O, int ncell,
                           int g, int alloc_slots) {
   k_bool_window<<<1, 1024, 0, c.stream>>>(op, A, B, O, ncell, g, c.st);
-  k_tile_cells<<<c.work_blocks, 256, 0, c.stream>>>(O, c.st);
+  k_tile_descs<<<c.work_blocks, 256, 0, c.stream>>>(op, A, B, O, c.st);
   if (!alloc_slots) return;
   k_pool_alloc<<<1, 1, 0, c.stream>>>(A, op == GB_OP_MERGE ? nullptr : B, O, c.cap_factor, c.st);
 }

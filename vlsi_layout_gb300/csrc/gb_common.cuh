@@ -51,6 +51,13 @@ struct DStatus {          // one per context, in device memory
   char* arena_base;
 };
 
+// A Boolean result's tile: its cell and where the operands' pieces of that
+// tile start (offsets into their piece arrays).
+struct TileDesc {
+  int cell, nA, nB, pad;
+  long long offA, offB;
+};
+
 struct DLayer {
   // common
   int ncell;
@@ -74,7 +81,7 @@ struct DLayer {
   long long nused;         // pool cursor (Boolean results reserve per tile from it)
   long long ntot;          // pieces held by the layer
   int4* cbox;              // [ncell] bounding box (raw and binned)
-  int* tcell;              // [ntiles] cell of each tile (Boolean results; null elsewhere: search tbase)
+  TileDesc* tdesc;         // [ntiles] Boolean results: each tile's cell and operand pieces (else null)
 };
 
 __host__ __device__ inline unsigned long long gb_pack(int x1, int y1, int x2, int y2) {

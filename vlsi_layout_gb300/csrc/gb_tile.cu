@@ -30,8 +30,9 @@
 //     row 1 with no change from row 0 are "continuations".  The scan pass
 //     leaves each column's local prefix of the recurrence, the count pass
 //     each column's piece starts, so the passes after them do not evaluate
-//     it again.  A piece's 16-byte record goes to the CTA's record region at
-//     the piece's index.
+//     it again.  The pieces are dealt to the lanes 32 at a time in (column,
+//     row) order, so a column with many pieces does not hold up the warp; a
+//     piece's 16-byte record goes to the CTA's record region at its index.
 //  D. Stitch.  The records come into shared memory in one bulk copy.  Each
 //     continuation is linked to the open piece of the previous sub-band with
 //     the same y-interval; every chain head becomes one strip.  The output
@@ -226,7 +227,8 @@ __device__ __forceinline__ void* sc_up(TileSmem& s, char* base, unsigned long lo
 }
 
 
-// Output tile t: its cell, and where A's and B's pieces of that tile start.
+// Output tile t: its cell, and where A's and B's pieces of that tile start.  A Boolean result carries a
+// descriptor per tile (one load); other callers' layers are looked up through the cell windows.
 __device__ __forceinline__ void tile_lookup(int op, const DLayer* A, const DLayer* B, const DLayer* O, long long t,
                                             TileRef& r) {
   r.tile = t;
@@ -234,7 +236,16 @@ __device__ __forceinline__ void tile_lookup(int op, const DLayer* A, const DLaye
   r.pa = r.pb = nullptr;
   r.cell = 0;
   if (t >= O->ntiles) return;
-  const int k = O->tcell ? O->tcell[t] : gb_find_cell(O->tbase, O->ncell, t);
+  if (O->tdesc) {
+    const TileDesc d = O->tdesc[t];
+    r.cell = d.cell;
+    r.nA = d.nA;
+    r.nB = d.nB;
+    if (d.nA) r.pa = A->pcs + d.offA;
+    if (d.nB) r.pb = B->pcs + d.offB;
+    return;
+  }
+  const int k = gb_find_cell(O->tbase, O->ncell, t);
   const int4 w = O->win[k];
   const long long li = t - O->tbase[k];
   const int tx = w.x + (int)(li % w.z), ty = w.y + (int)(li / w.z);
@@ -580,19 +591,45 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   int* olist = (int*)obase;  // open pieces, then continuation pieces, each in y order
   TSTEP(3)
 
-  // ---- write pieces
+  // ---- write pieces, dealt to the lanes 32 at a time in (column, row) order: piece k's lane is found by a
+  // shuffle search over the lanes' piece counts, its column by a walk over that lane's columns, its row as
+  // its rank among the column's piece starts
   {
-    int p = pbase + posP, o = posO, h = posH, q = posC, z = posZ;
-    for (int c = c0; c < c1e; ++c) {
-      const unsigned long long Rc = ca[c], Rp1 = R(c + 1);
-      const unsigned long long Ec = Rc & ~Rp1;
-      const unsigned long long zs = cb[c];
-      const unsigned long long Z = zs & ~1ull;
-      const unsigned long long Chg = zs << 1;  // only its bit 1 is read below
-      unsigned long long Zr = Z;
-      while (Zr) {
+    const int inclP = posP + np;
+    for (int k0 = 0; k0 < totP; k0 += 32) {  // warp-uniform trip count
+      const int k = k0 + lane;
+      int ow = 0;  // owner lane: the first lane whose inclusive piece prefix exceeds k
+#pragma unroll
+      for (int st2 = 16; st2 > 0; st2 >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, inclP, ow + st2 - 1);
+        if (v <= k) ow += st2;
+      }
+      const int oP = __shfl_sync(0xffffffffu, posP, ow), oO = __shfl_sync(0xffffffffu, posO, ow);
+      const int oH = __shfl_sync(0xffffffffu, posH, ow), oC = __shfl_sync(0xffffffffu, posC, ow);
+      const int oZ = __shfl_sync(0xffffffffu, posZ, ow);
+      if (k < totP) {
+        int j = k - oP, o = oO, h = oH, q = oC, z = oZ;
+        int c = min(L, ow * per);
+        unsigned long long zs, Z, Ec;
+        int contc;
+        for (;;) {  // the owner's columns before the piece's own: their pieces, opens, continuations, row-0 ends
+          zs = cb[c];
+          Z = zs & ~1ull;
+          Ec = ca[c] & ~R(c + 1);
+          contc = (sb > 0) && ((Z >> 1) & 1ull) && !(zs & 1ull);
+          const int pc = __popcll(Z);
+          if (j < pc) break;
+          j -= pc;
+          h += pc - contc;
+          q += contc;
+          o += (!last_sb && (Ec >> 63)) ? 1 : 0;
+          z += (int)(Ec & 1ull);
+          ++c;
+        }
+        unsigned long long Zr = Z;
+        for (int i = 0; i < j; ++i) Zr &= Zr - 1;
         const int r = __ffsll((long long)Zr) - 1;
-        Zr &= Zr - 1;
+        h += j - ((contc && r > 1) ? 1 : 0);  // the column's continuation (row 1) is not a head
         const unsigned long long above = (r >= 63) ? 0ull : ((Z | ~Ec) & (~0ull << (r + 1)));
         const int rend = above ? (__ffsll((long long)above) - 1) : 64;
         int cs = c;
@@ -608,21 +645,19 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
             --cs;
           }
         }
-        const int cont = (sb > 0) && (r == 1) && !((Chg >> 1) & 1ull);
+        const int cont = (r == 1) && contc;
         const int open = (rend == 64) && !last_sb;
+        const int p = pbase + k;
         PieceRec pr;
         const unsigned hr = cont ? (unsigned)z : (unsigned)h;  // continuations keep their row-0 ordinal
         pr.x = lv[cs] | (cont << 30) | (open << 31);
         pr.y = lv[c + 1] | (int)((hr & 0x7fffu) << 17);
         pr.z = (rowbase + r) | (int)((hr >> 15) << 17);
         pr.w = rowbase + rend;
-        if (!cont) ++h;
-        recs[p - pbase] = pr;
-        if (open) olist[o++] = p;
-        if (cont) olist[totO + q++] = p;
-        ++p;
+        recs[k] = pr;
+        if (open) olist[o] = p;
+        if (cont) olist[totO + q] = p;
       }
-      z += (int)(Ec & 1ull);
     }
   }
   TSTEP(4)
@@ -958,8 +993,8 @@ k_tile(int op, const DLayer* A, const DLayer* B, DLayer* O, int g, int mode, cha
       }
       continue;
     }
-    // the next tile's reservation and lookups (a chain of dependent loads) run on the last thread while
-    // the others stitch and emit this tile
+    // the next tile's reservation (the work counter) and its descriptor load run on the last thread while
+    // the bulk copies below land
     if (tid == TK_NT - 1 && !st->err) {
       tile_lookup(op, A, B, O, (long long)atomicAdd((unsigned long long*)counter, 1ull), s.nx);
       s.have_nx = 1;
