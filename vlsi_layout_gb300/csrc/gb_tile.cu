@@ -555,11 +555,30 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   int totP, totO, totH, totC, totZ;
   // runs at row 0 are the runs at row 63 of the previous sub-band, both in y
   // order: a continuation's ordinal among them indexes that sub-band's open list
-  const int posZ = gb_warp_excl(nz, &totZ);
-  const int posP = gb_warp_excl(np, &totP);
-  const int posO = gb_warp_excl(no, &totO);
-  const int posH = gb_warp_excl(nh, &totH);
-  const int posC = gb_warp_excl(ncn, &totC);
+  int posZ, posP, posO, posH, posC;
+  if (L <= 512) {  // one 64-bit scan: pieces and heads (at most 64 x 512 each), opens, continuations, row-0 ends (at most 512)
+    const unsigned long long v = (unsigned long long)np | ((unsigned long long)nh << 16) |
+                                 ((unsigned long long)no << 32) | ((unsigned long long)ncn << 42) |
+                                 ((unsigned long long)nz << 52);
+    unsigned long long t;
+    const unsigned long long e = gb_warp_excl(v, &t);
+    posP = (int)(e & 0xffffu);
+    posH = (int)((e >> 16) & 0xffffu);
+    posO = (int)((e >> 32) & 0x3ffu);
+    posC = (int)((e >> 42) & 0x3ffu);
+    posZ = (int)((e >> 52) & 0x3ffu);
+    totP = (int)(t & 0xffffu);
+    totH = (int)((t >> 16) & 0xffffu);
+    totO = (int)((t >> 32) & 0x3ffu);
+    totC = (int)((t >> 42) & 0x3ffu);
+    totZ = (int)((t >> 52) & 0x3ffu);
+  } else {
+    posZ = gb_warp_excl(nz, &totZ);
+    posP = gb_warp_excl(np, &totP);
+    posO = gb_warp_excl(no, &totO);
+    posH = gb_warp_excl(nh, &totH);
+    posC = gb_warp_excl(ncn, &totC);
+  }
   int pbase = 0;
   unsigned long long obase = 0, rbase = 0;
   if (lane == 0) {
