@@ -149,26 +149,43 @@ __global__ void k_count_tiles(const DLayer* L, long long* per_cell, int ncell, D
   }
 }
 
-__global__ void k_morton_keys(const int4* b, long long n, unsigned long long* keys, unsigned* vals) {
+// ComputeMorton (gpu_morton.cu:113-144): the box centre's coordinates with the
+// sign bit flipped, x in the even bits and y in the odd bits.
+__device__ __forceinline__ unsigned long long morton_key(const int4 q) {
+  const unsigned cx = (unsigned)(((long long)q.x + q.z) / 2) ^ 0x80000000u;
+  const unsigned cy = (unsigned)(((long long)q.y + q.w) / 2) ^ 0x80000000u;
+  unsigned long long mx = cx, my = cy;
+  mx = (mx | (mx << 16)) & 0x0000FFFF0000FFFFull;
+  mx = (mx | (mx << 8)) & 0x00FF00FF00FF00FFull;
+  mx = (mx | (mx << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  mx = (mx | (mx << 2)) & 0x3333333333333333ull;
+  mx = (mx | (mx << 1)) & 0x5555555555555555ull;
+  my = (my | (my << 16)) & 0x0000FFFF0000FFFFull;
+  my = (my | (my << 8)) & 0x00FF00FF00FF00FFull;
+  my = (my | (my << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  my = (my | (my << 2)) & 0x3333333333333333ull;
+  my = (my | (my << 1)) & 0x5555555555555555ull;
+  return (my << 1) | mx;
+}
+
+// Keys and the identity payload; with orx, also the OR of every key with the
+// first key (the span the sort's passes must cover), so the sort needs no
+// separate read of the keys for it.
+__global__ void k_morton_keys(const int4* b, long long n, unsigned long long* keys, unsigned* vals,
+                              unsigned long long* orx = nullptr) {
+  unsigned long long acc = 0;
+  const unsigned long long k0 = (orx && n > 0) ? morton_key(b[0]) : 0ull;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const int4 q = b[i];
-    // ComputeMorton (gpu_morton.cu:113-144)
-    const unsigned cx = (unsigned)(((long long)q.x + q.z) / 2) ^ 0x80000000u;
-    const unsigned cy = (unsigned)(((long long)q.y + q.w) / 2) ^ 0x80000000u;
-    unsigned long long mx = cx, my = cy;
-    mx = (mx | (mx << 16)) & 0x0000FFFF0000FFFFull;
-    mx = (mx | (mx << 8)) & 0x00FF00FF00FF00FFull;
-    mx = (mx | (mx << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    mx = (mx | (mx << 2)) & 0x3333333333333333ull;
-    mx = (mx | (mx << 1)) & 0x5555555555555555ull;
-    my = (my | (my << 16)) & 0x0000FFFF0000FFFFull;
-    my = (my | (my << 8)) & 0x00FF00FF00FF00FFull;
-    my = (my | (my << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    my = (my | (my << 2)) & 0x3333333333333333ull;
-    my = (my | (my << 1)) & 0x5555555555555555ull;
-    keys[i] = (my << 1) | mx;
+    const unsigned long long k = morton_key(b[i]);
+    keys[i] = k;
     vals[i] = (unsigned)i;
+    acc |= k ^ k0;
+  }
+  if (orx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicOr(orx, acc);
   }
 }
 
@@ -948,16 +965,22 @@ extern "C" int gb_component_areas(gb_context* ctx, const c_box* boxes, unsigned 
 }
 
 // ======================================================================= sorts
-static int sort_keys_perm(gb_context* ctx, unsigned long long* dkeys, unsigned* dvals, long long n) {
+// Sorts keys with their payloads over the key bits that differ.  d_span, when
+// given, already holds the OR of every key with the first key (computed where
+// the keys were made); otherwise one pass over the keys computes it.
+static int sort_keys_perm(gb_context* ctx, unsigned long long* dkeys, unsigned* dvals, long long n,
+                          unsigned long long* d_span = nullptr) {
   GbCtx& c = ctx->c;
-  unsigned long long* orx = nullptr;
-  cudaMalloc(&orx, 8);
-  cudaMemsetAsync(orx, 0, 8, c.stream);
-  k_key_span<<<c.work_blocks, 256, 0, c.stream>>>(dkeys, n, orx);
+  unsigned long long* orx = d_span;
+  if (!orx) {
+    cudaMalloc(&orx, 8);
+    cudaMemsetAsync(orx, 0, 8, c.stream);
+    k_key_span<<<c.work_blocks, 256, 0, c.stream>>>(dkeys, n, orx);
+  }
   unsigned long long span = 0;
   cudaMemcpyAsync(&span, orx, 8, cudaMemcpyDeviceToHost, c.stream);
   cudaStreamSynchronize(c.stream);
-  cudaFree(orx);
+  if (!d_span) cudaFree(orx);
   int bits = 0;
   while (bits < 64 && (span >> bits)) ++bits;
   if (bits == 0) return GB_OK;
@@ -995,13 +1018,15 @@ static int morton_sort_impl(gb_context* ctx, c_box* boxes, long long n, int sort
   int e = GB_OK;
   if (dev_io) db = (int4*)boxes;
   else if (cudaMalloc(&db, (size_t)n * 16) != cudaSuccess) return GB_ERR_OOM;
-  if (cudaMalloc(&dk, (size_t)n * 8) != cudaSuccess || cudaMalloc(&dv, (size_t)n * 4) != cudaSuccess) {
+  // keys, then one word for their span
+  if (cudaMalloc(&dk, (size_t)(n + 1) * 8) != cudaSuccess || cudaMalloc(&dv, (size_t)n * 4) != cudaSuccess) {
     e = GB_ERR_OOM;
     goto done;
   }
   if (!dev_io) cudaMemcpyAsync(db, boxes, (size_t)n * 16, cudaMemcpyHostToDevice, c.stream);
-  k_morton_keys<<<c.work_blocks, 256, 0, c.stream>>>(db, n, dk, dv);
-  e = sort_keys_perm(ctx, dk, dv, n);
+  cudaMemsetAsync(dk + n, 0, 8, c.stream);
+  k_morton_keys<<<c.work_blocks, 256, 0, c.stream>>>(db, n, dk, dv, dk + n);
+  e = sort_keys_perm(ctx, dk, dv, n, dk + n);
   if (e) goto done;
   if (keys_out) cudaMemcpy(keys_out, dk, (size_t)n * 8, dev_io ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
   if (perm_out) {
