@@ -275,7 +275,12 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   const int lane = gb_lane(), wid = gb_warp();
   long long q0 = tctr ? clock64() : 0;
   const long long qstart = q0;
-#define TSTEP(k) if (tctr && lane == 0) { const long long q1 = clock64(); atomicAdd((unsigned long long*)&tctr[k], (unsigned long long)(q1 - q0)); q0 = q1; }
+#define TSTEP(k)                                                           \
+  if (tctr && lane == 0) {                                                 \
+    const long long q1 = clock64();                                        \
+    atomicAdd((unsigned long long*)&tctr[k], (unsigned long long)(q1 - q0)); \
+    q0 = q1;                                                               \
+  }
   const unsigned long long half = scr >> 1;
   const int beg = sb ? s.sbc[sb - 1] : 0, end = s.sbc[sb];
   const int m = end - beg;
@@ -556,7 +561,9 @@ __device__ void tile_subband(TileSmem& s, int op, int sb, int nsb, int Ny, int n
   // runs at row 0 are the runs at row 63 of the previous sub-band, both in y
   // order: a continuation's ordinal among them indexes that sub-band's open list
   int posZ, posP, posO, posH, posC;
-  if (L <= 512) {  // one 64-bit scan: pieces and heads (at most 64 x 512 each), opens, continuations, row-0 ends (at most 512)
+  // one 64-bit scan when the fields cannot overflow: pieces and heads (at most 64 x 512 each) in 16 bits,
+  // opens, continuations and row-0 ends (at most 512 each) in 10 bits
+  if (L <= 512) {
     const unsigned long long v = (unsigned long long)np | ((unsigned long long)nh << 16) |
                                  ((unsigned long long)no << 32) | ((unsigned long long)ncn << 42) |
                                  ((unsigned long long)nz << 52);
