@@ -59,7 +59,8 @@
 #define TK_LVN 256
 #define TK_LCN 128
 #define TK_MC 128   // sub-band members kept in the per-warp member cache (8 bytes each)
-#define TK_MLD 4    // member records loaded per lane before the first is used
+#define TK_MLD 2    // member records loaded per lane before the first is used (per 1024-cell deck: 4 -> 2
+                    // records 30.88 -> 30.59 ms)
 #define TK_LD 2     // independent global loads in flight per thread in the streaming loops
 #define TK_DIRECT 1 // columns of a member painted on its own lane; the rest are spread over the warp
                     // (measured per 1024-cell deck: 0 / 1 / 2 / 3 / 4 / 8 columns -> 35.16 / 34.78 /
