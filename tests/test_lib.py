@@ -34,3 +34,15 @@ def test_engine_refuses_without_library(tmp_path, monkeypatch):
         assert "no CPU fallback" in str(e)
     else:
         raise AssertionError("engine loaded without its library")
+
+
+def test_bench_reads_committed_profile_traffic():
+    # the bench line's roofline.traffic comes from the committed ncu summary of
+    # the scanline kernel; a summary without a parsable figure would drop it
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    t = bench.ncu_traffic()
+    assert t is not None and t > 1e8
+    peak, kind = bench.peaks()
+    assert peak > 1000 and kind in ("measured", "fallback")
