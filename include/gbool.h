@@ -127,7 +127,8 @@ int gb_arena_release(gb_context* ctx, unsigned long long mark);
 /* Output pool of a Boolean op, in pieces per input piece (default 2; doubled
  * and retried automatically by the host-synchronous entry points). */
 int gb_set_capacity_factor(gb_context* ctx, int factor);
-/* Per-CTA scratch of the tile kernel in bytes (default 8 MiB). */
+/* Per-CTA scratch of the tile kernel in bytes (default 8 MiB; at least 64 KiB,
+ * rounded up to a multiple of 512). */
 int gb_set_tile_scratch(gb_context* ctx, unsigned long long bytes);
 
 /* A layer of n boxes (host pointer), grouped into ncell independent cells by

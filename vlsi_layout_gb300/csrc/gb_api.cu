@@ -434,7 +434,9 @@ extern "C" int gb_set_capacity_factor(gb_context* ctx, int factor) {
 
 extern "C" int gb_set_tile_scratch(gb_context* ctx, unsigned long long bytes) {
   if (!ctx || bytes < (1ull << 16)) return GB_ERR_ARG;
-  return realloc_scratch(ctx, (size_t)bytes);
+  // every CTA's scratch (and its upper half, the record region) starts on 256 bytes: the tile kernel's bulk
+  // copies and 16-byte records need 16-byte aligned addresses
+  return realloc_scratch(ctx, (size_t)((bytes + 511ull) & ~511ull));
 }
 
 // ======================================================================= layers
