@@ -1257,7 +1257,7 @@ void gb_launch_tile_bool(GbCtx& c, int op, const DLayer* A, const DLayer* B, DLa
 // Set-up: the first call on a device resolves the device addresses of the
 // static storage with cudaGetSymbolAddress (with that device current) and
 // sets the kernel's shared-memory attribute; later calls on that device reuse
-// them.  Make that first call before any stream capture.
+// them.
 #define GB_NA_MAX_IN 16384
 #define GB_NA_MAX_OUT 65536
 #define GB_NA_SCRATCH (8u << 20)
