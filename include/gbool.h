@@ -253,10 +253,9 @@ int32_t gb_um_to_dbu(double r);
  * GB_ERR_CAPACITY too.  Boxes outside the first box's tile give
  * GB_ERR_INVALID_BOX.  On every status other than GB_OK, *d_count (and
  * *d_area) is -1.  The first call on a device sets up the static storage
- * (cudaGetSymbolAddress).  All
- * calls share that storage: calls whose GPU work overlaps race.  Every call
- * waits for `stream` (a cudaStream_t, NULL = default) to finish and returns
- * the status. */
+ * (cudaGetSymbolAddress).  All calls share that storage: calls whose GPU
+ * work overlaps race.  Every call waits for `stream` (a cudaStream_t, NULL =
+ * default) to finish and returns the status. */
 int gb_bool_tile_noalloc(int op, const c_box* d_A, int nA, const c_box* d_B, int nB, c_box* d_out,
                          long long out_cap, long long* d_count, long long* d_area, void* stream);
 
